@@ -1,0 +1,277 @@
+"""Benchmark of the GB300 streaming BDPT (plain "BDPTSC" mode).
+
+Workload: the 1024x768 interior scene (20x10x30 room, 180 icospheres,
+57,614 triangles), eye and light depth caps 10, one progressive frame per
+step (786,432 camera paths), Philox seed 1234.  Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle restatement, multithreaded over the machine's host cores) on the same
+workload: the reference's own code is Windows/MSVC + CUDA 7.5 texture
+references and does not build here.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "BDPT Mpaths/s"
+WORKLOAD = "plain streaming BDPT, procedural interior 20x10x30 room + 180 icospheres (57,614 tris), 1024x768, depth 10"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def scene_and_camera():
+    from cudapt_gb300 import scenes
+    return scenes.interior()
+
+
+def params_for(gb_or_layouts):
+    return gb_or_layouts.default_params(eye_depth_max=10, light_depth_max=10)
+
+
+W, H = 1024, 768
+
+
+def run_cpu_sample(threads, rows, frames=1, seed=1234):
+    """Oracle (CPU restatement of the reference estimator) on a band of rows of
+    the same workload; returns (paths, seconds, build_seconds)."""
+    import oracle
+    from cudapt_gb300 import layouts
+    (v, t, m), cam = scene_and_camera()
+    sc = oracle.Scene(v, t, m)
+    p = layouts.default_params(eye_depth_max=10, light_depth_max=10, seed=seed)
+    # a band of `rows` full-width rows: same pixels-per-path cost as the full frame
+    band_cam = dict(cam)
+    r = oracle.Renderer(W, rows, 0, p, threads=threads)
+    t0 = time.perf_counter()
+    r.render(sc, band_cam, frames)
+    dt = time.perf_counter() - t0
+    return W * rows * frames, dt, sc.build_seconds
+
+
+def bench_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    # bounded sample per step: a 1024 x rows band; rows sized for ~10 s per step
+    rows = int(os.environ.get("GBPT_REF_ROWS", "48"))
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        run_cpu_sample(threads, 4)
+    paths = secs = 0.0
+    for _ in range(args.steps):
+        p, dt, build_s = run_cpu_sample(threads, rows)
+        paths += p
+        secs += dt
+    v = paths / secs / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Mpaths/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "width": W, "height": H, "paths_per_step": W * rows,
+                   "sample": f"1024x{rows} row band per step (full-width rows of the same frame)"},
+        "cpu_baseline": {"value": round(v, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
+                         "sample": f"1024x{rows} band x {args.steps} steps, oracle FP32 estimator + restated BVH build "
+                                   f"({build_s:.2f} s build)"},
+        "e2e": {"value": round(v, 4), "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def bench_gpu(args):
+    rank, world, local = dist_env()
+    import cudapt_gb300 as gb
+    from cudapt_gb300 import build as gbuild
+    gbuild.build()
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    if not gb.device_available():
+        raise SystemExit("bench: no usable CUDA device")
+    (v, t, m), cam = scene_and_camera()
+    scene = gb.RTScene(v, t, m).build_bvh()
+    build_s = scene.build_seconds
+    params = params_for(gb)
+    np_ = W * H
+    r = gb.RTRenderer(W, H, gb.MODE_BDPT_SC, params)
+
+    flush = FlushBuffer()
+    # warm-up
+    for _ in range(max(args.warmup, 0)):
+        r.render_frames(scene, cam, 1, stats=True)
+    # timed: one frame per step, L2 flushed (256 MB device memset) before each
+    ms = []
+    phases = {"ms_trace": 0.0, "ms_shade": 0.0, "ms_shadow": 0.0, "ms_light": 0.0}
+    rays = 0
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush()
+            st = r.render_frames(scene, cam, 1, stats=True)
+            ms.append(st["ms_total"])
+            rays += st["rays"]
+            for k in phases:
+                phases[k] += st[k]
+    total_ms = float(np.sum(ms))
+    value = args.steps * np_ / (total_ms / 1e3) / 1e6
+
+    # e2e through the public call with a host result buffer (D2H of the image each step)
+    out = np.zeros(np_ * 3, np.float32)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r.render(scene, cam, stats=False)
+    e2e_s = time.perf_counter() - t0
+    e2e = args.steps * np_ / e2e_s / 1e6
+
+    # work counters for the roofline (separate, untimed frame)
+    r.set_counting(True)
+    cst = r.render_frames(scene, cam, 1, stats=True)
+    r.set_counting(False)
+    trace_bytes = 40 * cst["nodes"] + 48 * cst["tris"]
+    trace_ms = cst["ms_trace"]
+    achieved = trace_bytes / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else None
+    peak, peak_kind = load_peaks()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rows = int(os.environ.get("GBPT_CPU_ROWS", "24"))
+        p, dt, bs = run_cpu_sample(threads, rows)
+        cpu = {"value": round(p / dt / 1e6, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
+               "sample": f"1024x{rows} row band of one frame, oracle FP32 estimator ({bs:.2f} s restated BVH build)"}
+
+    launches_per_frame = 1 + 3 * int(params["eye_depth_max"]) + 1
+    light_frames = sum(1 for f in range(args.warmup, args.warmup + args.steps)
+                       if f % int(params["light_every"]) == 0)
+    line = {
+        "metric": METRIC, "value": round(value * world, 3), "unit": "Mpaths/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (procedural scene, seeded)",
+        "config": {"workload": WORKLOAD, "width": W, "height": H, "paths_per_step": np_,
+                   "eye_depth_max": 10, "light_depth_max": 10, "tris": int(len(t)),
+                   "l2": "flushed before every timed step (256 MB device memset)",
+                   "bvh_build_s": round(build_s, 4), "rays_per_s": round(rays / (total_ms / 1e3), 1),
+                   "phase_ms_per_step": {k: round(v_ / args.steps, 4) for k, v_ in phases.items()},
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": round(e2e * world, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": 40,
+                "d2h_bytes_per_step": np_ * 12},
+        "roofline": {"bound": "hbm", "kernel": "k_trace (closest-hit BVH walk)",
+                     "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4) if achieved else None, "peak_kind": peak_kind,
+                     "traffic": None,
+                     "algorithmic_bytes_per_frame": int(trace_bytes)},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps * launches_per_frame + light_frames,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+class FlushBuffer:
+    """Writes 256 MB of device memory (twice the 126 MB L2) before a step."""
+
+    def __init__(self):
+        import torch
+        self.torch = torch
+        self.buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def __call__(self):
+        self.buf.fill_(1.0)
+        self.torch.cuda.synchronize()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbpt", choices=["gbpt", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        bench_reference(args)
+    else:
+        bench_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

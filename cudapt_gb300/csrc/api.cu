@@ -1,0 +1,966 @@
+// C ABI of libgbpt: scenes, renderers and the per-frame launch sequence.
+//
+// Replaces RTScene / RTRenderer (include/raytracer.h:228-323) and the
+// per-renderer Render functions (src/cudaRTBDPTStream.cu:816-951,
+// src/cudaRTBDPTStreamAdapBilatAtomic.cu:1253-1554) for the BDPT modes.
+// Unlike the reference there is no process-global device state: every scene
+// and renderer owns its buffers, and a renderer owns its CUDA stream.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "gbpt_internal.h"
+#include "gbpt_math.cuh"
+#include "launch.h"
+
+using namespace gbpt;
+
+namespace gbpt {
+static thread_local std::string g_err;
+void set_error(const std::string& s) { g_err = s; }
+gbpt_status fail(gbpt_status st, const std::string& s) {
+  g_err = s;
+  return st;
+}
+}  // namespace gbpt
+
+#define CK(call)                                                                                 \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess)                                                                       \
+      return fail(e_ == cudaErrorMemoryAllocation ? GBPT_ERR_OOM : GBPT_ERR_CUDA,                \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                           \
+  } while (0)
+
+namespace {
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  return cudaMalloc((void**)p, n * sizeof(T));
+}
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+uint64_t g_sceneVersion = 1;
+std::mutex g_versionMu;
+uint64_t next_version() {
+  std::lock_guard<std::mutex> l(g_versionMu);
+  return ++g_sceneVersion;
+}
+
+}  // namespace
+
+struct gbpt_scene {
+  std::vector<gbpt_vertex> verts;
+  std::vector<gbpt_triangle> tris;  // caller order
+  std::vector<gbpt_material> mats;
+  HostBVH bvh;
+  bool built = false;
+  std::vector<gbpt_triangle> trisOrdered;
+  std::vector<uint32_t> lightTri;
+  float4 *dNodes = nullptr, *dTris = nullptr, *dShade = nullptr, *dMats = nullptr;
+  uint32_t* dLight = nullptr;
+  DevScene dev;
+  uint64_t version = 0;
+  bool uploaded = false;
+
+  void free_dev() {
+    dfree(dNodes);
+    dfree(dTris);
+    dfree(dShade);
+    dfree(dMats);
+    dfree(dLight);
+    dev = DevScene{};
+  }
+  ~gbpt_scene() { free_dev(); }
+};
+
+namespace {
+
+// src/cudaRTBDPTStream.cu:57-77 -- host length of the emissive colour > 0
+void scan_lights(gbpt_scene* s) {
+  s->lightTri.clear();
+  for (uint32_t i = 0; i < s->trisOrdered.size(); i++) {
+    const float* e = s->mats[s->trisOrdered[i].mat].emissive;
+    if (std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) > 0.f) s->lightTri.push_back(i);
+  }
+}
+
+std::vector<float4> pack_materials(const std::vector<gbpt_material>& mats) {
+  std::vector<float4> m(mats.size() * 3);
+  for (size_t i = 0; i < mats.size(); i++) {
+    const gbpt_material& a = mats[i];
+    m[3 * i] = make_float4(a.diffuse[0], a.diffuse[1], a.diffuse[2], a.transparency);
+    m[3 * i + 1] = make_float4(a.emissive[0], a.emissive[1], a.emissive[2], a.specular);
+    m[3 * i + 2] = make_float4(a.metallic, a.roughness, 0.f, 0.f);
+  }
+  return m;
+}
+
+float as_f(uint32_t u) {
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+gbpt_status upload_scene(gbpt_scene* s) {
+  s->free_dev();
+  const uint32_t nt = (uint32_t)s->trisOrdered.size(), nn = s->bvh.nodeN;
+  std::vector<float4> nodes((size_t)nn * 2), tris((size_t)nt * 3), shade((size_t)nt * 5);
+  for (uint32_t i = 0; i < nn; i++) {
+    const float* b = &s->bvh.bounds[(size_t)i * 6];
+    nodes[2 * i] = make_float4(b[0], b[1], b[2], as_f(s->bvh.offOrTSTN[2 * i]));
+    nodes[2 * i + 1] = make_float4(b[3], b[4], b[5], as_f(s->bvh.offOrTSTN[2 * i + 1]));
+  }
+  for (uint32_t i = 0; i < nt; i++) {
+    const gbpt_triangle& t = s->trisOrdered[i];
+    const gbpt_vertex &a = s->verts[t.v0], &b = s->verts[t.v1], &c = s->verts[t.v2];
+    // src/cudaRTCommon.cu:507-509: p0, p1 - p0, p2 - p0 (host float subtraction)
+    tris[3 * i] = make_float4(a.pos[0], a.pos[1], a.pos[2], 0.f);
+    tris[3 * i + 1] = make_float4(b.pos[0] - a.pos[0], b.pos[1] - a.pos[1], b.pos[2] - a.pos[2], 0.f);
+    tris[3 * i + 2] = make_float4(c.pos[0] - a.pos[0], c.pos[1] - a.pos[1], c.pos[2] - a.pos[2], 0.f);
+    shade[5 * i] = make_float4(a.norm[0], a.norm[1], a.norm[2], a.pos[0]);
+    shade[5 * i + 1] = make_float4(b.norm[0], b.norm[1], b.norm[2], a.pos[1]);
+    shade[5 * i + 2] = make_float4(c.norm[0], c.norm[1], c.norm[2], a.pos[2]);
+    shade[5 * i + 3] = make_float4(b.pos[0], b.pos[1], b.pos[2], as_f(t.mat));
+    shade[5 * i + 4] = make_float4(c.pos[0], c.pos[1], c.pos[2], 0.f);
+  }
+  std::vector<float4> mats = pack_materials(s->mats);
+  CK(dalloc(&s->dNodes, nodes.size()));
+  CK(dalloc(&s->dTris, tris.size()));
+  CK(dalloc(&s->dShade, shade.size()));
+  CK(dalloc(&s->dMats, mats.size()));
+  CK(dalloc(&s->dLight, s->lightTri.size()));
+  CK(cudaMemcpy(s->dNodes, nodes.data(), nodes.size() * 16, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->dTris, tris.data(), tris.size() * 16, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->dShade, shade.data(), shade.size() * 16, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->dMats, mats.data(), mats.size() * 16, cudaMemcpyHostToDevice));
+  if (!s->lightTri.empty())
+    CK(cudaMemcpy(s->dLight, s->lightTri.data(), s->lightTri.size() * 4, cudaMemcpyHostToDevice));
+  s->dev.nodes = s->dNodes;
+  s->dev.tris = s->dTris;
+  s->dev.shade = s->dShade;
+  s->dev.mats = s->dMats;
+  s->dev.lightTri = s->dLight;
+  s->dev.nodeN = nn;
+  s->dev.triN = nt;
+  s->dev.lightN = (uint32_t)s->lightTri.size();
+  s->dev.matN = (uint32_t)s->mats.size();
+  s->uploaded = true;
+  return GBPT_OK;
+}
+
+gbpt_status ensure_uploaded(gbpt_scene* s) {
+  if (!s->built) return fail(GBPT_ERR_STATE, "scene has no BVH (call gbpt_scene_build_bvh)");
+  if (s->uploaded) return GBPT_OK;
+  return upload_scene(s);
+}
+
+enum Phase { kPhLight = 0, kPhTrace, kPhShade, kPhShadow, kPhFilter, kPhAdapt, kPhOther, kPhN };
+
+}  // namespace
+
+struct gbpt_renderer {
+  uint32_t W = 0, H = 0;
+  int32_t mode = GBPT_MODE_BDPT_SC;
+  gbpt_params p{};
+  float debugMode = 0.f;
+  cudaStream_t st = nullptr;
+  bool alloc = false;
+  RenderBuffers rb{};
+  AdaptBuffers ab{};
+  float *result = nullptr, *gpos = nullptr, *gnorm = nullptr, *gdiff = nullptr, *gauss = nullptr;
+  uint32_t* sampleN = nullptr;
+  float4* waveMem = nullptr;
+  std::vector<float> hostResult;
+  uint32_t frame = 0;
+  bool started = false;
+  float camBasis[9] = {0};
+  uint64_t sceneVersion = 0;
+  bool counting = false;
+  float gaussKey[2] = {-1.f, -1.f};
+  std::vector<std::pair<int, cudaEvent_t>> evs;
+  std::vector<cudaEvent_t> evPool;
+
+  void free_dev() {
+    for (int k = 0; k < 2; k++) rb.wave[k] = Wave{};
+    dfree(waveMem);
+    dfree(rb.hit);
+    dfree(rb.sh);
+    dfree(rb.res);
+    dfree(rb.gbuf);
+    dfree(rb.slotPix);
+    dfree(rb.slotSmp);
+    dfree(rb.cache);
+    dfree(rb.ctr);
+    dfree(ab.err);
+    dfree(ab.cnt);
+    dfree(ab.off);
+    dfree(ab.blockSum);
+    dfree(ab.partial);
+    dfree(ab.filtered);
+    dfree(result);
+    dfree(gpos);
+    dfree(gnorm);
+    dfree(gdiff);
+    dfree(gauss);
+    dfree(sampleN);
+    alloc = false;
+  }
+  ~gbpt_renderer() {
+    if (st) cudaStreamSynchronize(st);
+    free_dev();
+    for (auto e : evPool) cudaEventDestroy(e);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+namespace {
+
+gbpt_status check_params(const gbpt_params* p) {
+  if (!p) return fail(GBPT_ERR_INVALID_ARG, "params is NULL");
+  if (p->eye_depth_max < 1 || p->eye_depth_max > 64) return fail(GBPT_ERR_INVALID_ARG, "eye_depth_max must be 1..64");
+  if (p->light_depth_max < 1 || p->light_depth_max > 64)
+    return fail(GBPT_ERR_INVALID_ARG, "light_depth_max must be 1..64");
+  if (p->light_paths > 1024) return fail(GBPT_ERR_INVALID_ARG, "light_paths must be <= 1024");
+  if (p->light_every < 1) return fail(GBPT_ERR_INVALID_ARG, "light_every must be >= 1");
+  if (p->filter_radius > 31) return fail(GBPT_ERR_INVALID_ARG, "filter_radius must be <= 31");
+  return GBPT_OK;
+}
+
+gbpt_status ensure_alloc(gbpt_renderer* r) {
+  if (r->alloc) return GBPT_OK;
+  const size_t np = (size_t)r->W * r->H;
+  const size_t cap = np;
+  const uint32_t cacheCap = std::max(1u, r->p.light_paths * (1 + r->p.light_depth_max));
+  // admission: refuse when the buffers cannot fit in free HBM
+  size_t need = cap * (128 + 16 + 48 + 16 + 48 + 8) + np * (12 * 5 + 4 + 4 * 4) + (size_t)cacheCap * 96;
+  size_t freeB = 0, totB = 0;
+  CK(cudaMemGetInfo(&freeB, &totB));
+  if (need + (64ull << 20) > freeB)
+    return fail(GBPT_ERR_OOM, "renderer needs " + std::to_string(need) + " bytes, " + std::to_string(freeB) +
+                                  " free");
+  CK(dalloc(&r->waveMem, cap * 8));
+  for (int k = 0; k < 2; k++) {
+    float4* b = r->waveMem + (size_t)k * 4 * cap;
+    r->rb.wave[k] = Wave{b, b + cap, b + 2 * cap, b + 3 * cap};
+  }
+  CK(dalloc(&r->rb.hit, cap));
+  CK(dalloc(&r->rb.sh, cap * 3));
+  CK(dalloc(&r->rb.res, cap));
+  CK(dalloc(&r->rb.gbuf, cap * 3));
+  CK(dalloc(&r->rb.slotPix, cap));
+  CK(dalloc(&r->rb.slotSmp, cap));
+  CK(dalloc(&r->rb.cache, (size_t)cacheCap * 6));
+  CK(dalloc(&r->rb.ctr, 1));
+  CK(cudaMemsetAsync(r->rb.ctr, 0, sizeof(DevCounters), r->st));
+  CK(cudaMemsetAsync(r->rb.cache, 0, (size_t)cacheCap * 96, r->st));
+  r->rb.cap = (uint32_t)cap;
+  r->rb.cacheCap = cacheCap;
+  CK(dalloc(&r->result, np * 3));
+  CK(dalloc(&r->gpos, np * 3));
+  CK(dalloc(&r->gnorm, np * 3));
+  CK(dalloc(&r->gdiff, np * 3));
+  CK(dalloc(&r->sampleN, np));
+  CK(dalloc(&r->gauss, 64));
+  CK(dalloc(&r->ab.err, np));
+  CK(dalloc(&r->ab.cnt, np));
+  CK(dalloc(&r->ab.off, np));
+  CK(dalloc(&r->ab.blockSum, adapt_scan_blocks((uint32_t)np)));
+  CK(dalloc(&r->ab.partial, adapt_reduce_blocks((uint32_t)np)));
+  CK(dalloc(&r->ab.filtered, np * 3));
+  for (float* b : {r->result, r->gpos, r->gnorm, r->gdiff, r->ab.filtered})
+    CK(cudaMemsetAsync(b, 0, np * 12, r->st));
+  CK(cudaMemsetAsync(r->sampleN, 0, np * 4, r->st));
+  CK(cudaMemsetAsync(r->ab.err, 0, np * 4, r->st));
+  r->hostResult.assign(np * 3, 0.f);
+  r->alloc = true;
+  r->gaussKey[0] = r->gaussKey[1] = -1.f;
+  return GBPT_OK;
+}
+
+// host camera basis, src/cudaRTBDPTStream.cu:823-824 (host Vec3 algebra)
+void cam_basis(const gbpt_camera& c, float right[3], float up[3]) {
+  const float* d = c.dir;
+  const float* u = c.up;
+  float r[3] = {d[1] * u[2] - d[2] * u[1], d[2] * u[0] - d[0] * u[2], d[0] * u[1] - d[1] * u[0]};
+  float l = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  for (int k = 0; k < 3; k++) right[k] = r[k] / l;
+  float q[3] = {right[1] * d[2] - right[2] * d[1], right[2] * d[0] - right[0] * d[2],
+                right[0] * d[1] - right[1] * d[0]};
+  l = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+  for (int k = 0; k < 3; k++) up[k] = q[k] / l;
+}
+
+void gaussian_table_host(float delta, uint32_t radius, float* g) {  // src/cudaBilateralFilter.cu:5-24
+  for (uint32_t i = 0; i < 2 * radius + 1; i++) {
+    int x = (int)i - (int)radius;
+    g[i] = gb::exp_p((float)(-(x * x)) / (2 * delta * delta));
+  }
+}
+
+cudaEvent_t mark(gbpt_renderer* r, int phase, bool timing) {
+  if (!timing) return nullptr;
+  cudaEvent_t e;
+  size_t used = r->evs.size();
+  if (used < r->evPool.size()) {
+    e = r->evPool[used];
+  } else {
+    cudaEventCreate(&e);
+    r->evPool.push_back(e);
+  }
+  cudaEventRecord(e, r->st);
+  r->evs.push_back({phase, e});
+  return e;
+}
+
+gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, bool timing) {
+  float right[3], up[3];
+  cam_basis(*cam, right, up);
+  float basis9[9] = {cam->pos[0], cam->pos[1], cam->pos[2], cam->dir[0], cam->dir[1],
+                     cam->dir[2], up[0],       up[1],       up[2]};
+  bool same = r->started && r->sceneVersion == s->version && std::memcmp(basis9, r->camBasis, sizeof(basis9)) == 0;
+  r->frame = same ? r->frame + 1 : 0;
+  std::memcpy(r->camBasis, basis9, sizeof(basis9));
+  r->started = true;
+  r->sceneVersion = s->version;
+
+  FrameArgs a{};
+  for (int k = 0; k < 3; k++) {
+    a.camPos[k] = cam->pos[k];
+    a.camDir[k] = cam->dir[k];
+    a.camUp[k] = up[k];
+    a.camRight[k] = right[k];
+  }
+  a.tanHalf = (float)std::tan((double)(cam->fov * 0.5f));
+  a.W = (float)r->W;
+  a.H = (float)r->H;
+  a.width = r->W;
+  a.height = r->H;
+  a.frame = r->frame;
+  a.key0 = r->p.seed;
+  a.key1 = r->p.request_id;
+  a.eyeDepth = r->p.eye_depth_max;
+  a.lightDepth = r->p.light_depth_max;
+  a.lightPaths = r->p.light_paths;
+  for (int k = 0; k < 3; k++) a.env[k] = r->p.env[k];
+  a.useEnv = (r->p.env[0] != 0.f || r->p.env[1] != 0.f || r->p.env[2] != 0.f) ? 1u : 0u;
+  const bool adaptive = r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT;
+  a.specPush = adaptive ? 1u : 0u;
+  a.gbuffer = adaptive ? 1u : 0u;
+  a.counting = r->counting ? 1u : 0u;
+  const DevScene& S = s->dev;
+  cudaStream_t st = r->st;
+
+  mark(r, kPhOther, timing);
+  if (r->frame % r->p.light_every == 0) {
+    CK(launch_light_pass(S, a, r->rb, st));
+    mark(r, kPhLight, timing);
+  }
+  const bool budgeted = adaptive && r->frame >= r->p.warmup_frames;
+  if (budgeted) {
+    float delta = r->p.filter_sigma_spatial > 0.f ? r->p.filter_sigma_spatial : r->p.filter_color_eud;
+    if (r->gaussKey[0] != delta || r->gaussKey[1] != (float)r->p.filter_radius) {
+      float g[64] = {0};
+      gaussian_table_host(delta, r->p.filter_radius, g);
+      CK(cudaMemcpyAsync(r->gauss, g, sizeof(g), cudaMemcpyHostToDevice, st));
+      r->gaussKey[0] = delta;
+      r->gaussKey[1] = (float)r->p.filter_radius;
+    }
+    CK(launch_bilateral(r->result, r->gpos, r->gnorm, r->p.filter_diffuse ? r->gdiff : nullptr, r->W, r->H,
+                        r->p.filter_color_eud, r->p.filter_pos_eud, r->p.filter_norm_eud, r->p.filter_diff_eud,
+                        r->p.filter_radius, r->gauss, r->ab.filtered, st));
+    mark(r, kPhFilter, timing);
+    CK(launch_adapt_budget(a, r->rb, r->ab, r->result, r->sampleN, r->p.desired_n, st));
+    mark(r, kPhAdapt, timing);
+  } else {
+    CK(launch_camera(a, r->rb, st));
+    mark(r, kPhOther, timing);
+  }
+  int in = 0;
+  for (uint32_t d = 0; d < r->p.eye_depth_max; d++) {
+    CK(launch_trace(S, a, r->rb, in, st));
+    mark(r, kPhTrace, timing);
+    CK(launch_shade(S, a, r->rb, in, d, st));
+    mark(r, kPhShade, timing);
+    CK(launch_shadow(S, a, r->rb, st));
+    mark(r, kPhShadow, timing);
+    in ^= 1;
+  }
+  if (budgeted) {
+    CK(launch_adapt_accum(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
+    mark(r, kPhAdapt, timing);
+  } else {
+    CK(launch_apply(a, r->rb, r->result, r->sampleN, adaptive ? r->gpos : nullptr, r->gnorm, r->gdiff, st));
+    mark(r, kPhOther, timing);
+  }
+  return GBPT_OK;
+}
+
+struct CtrSnap {
+  unsigned long long rays, nodes, tris;
+};
+
+gbpt_status read_ctr(gbpt_renderer* r, DevCounters* out) {
+  CK(cudaMemcpyAsync(out, r->rb.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, r->st));
+  CK(cudaStreamSynchronize(r->st));
+  return GBPT_OK;
+}
+
+gbpt_status render_impl(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, uint32_t frames, float* out,
+                        int32_t outDev, gbpt_stats* stats) {
+  if (!r || !s || !cam) return fail(GBPT_ERR_INVALID_ARG, "NULL renderer, scene or camera");
+  gbpt_status stt = ensure_uploaded(s);
+  if (stt != GBPT_OK) return stt;
+  stt = ensure_alloc(r);
+  if (stt != GBPT_OK) return stt;
+  DevCounters before{};
+  const bool timing = stats != nullptr;
+  if (timing) {
+    stt = read_ctr(r, &before);
+    if (stt != GBPT_OK) return stt;
+  }
+  r->evs.clear();
+  for (uint32_t f = 0; f < frames; f++) {
+    stt = frame_once(r, s, cam, timing);
+    if (stt != GBPT_OK) return stt;
+  }
+  const size_t np = (size_t)r->W * r->H;
+  if (out) {
+    const float* src = (r->debugMode == 4.f && r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT) ? r->ab.filtered : r->result;
+    CK(cudaMemcpyAsync(out, src, np * 12, outDev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, r->st));
+  }
+  CK(cudaStreamSynchronize(r->st));
+  CK(cudaGetLastError());
+  if (timing) {
+    DevCounters after{};
+    stt = read_ctr(r, &after);
+    if (stt != GBPT_OK) return stt;
+    std::memset(stats, 0, sizeof(*stats));
+    stats->frame = r->frame;
+    stats->light_vertices = after.cacheSize;
+    stats->paths = after.paths;
+    stats->rays = after.rays - before.rays;
+    stats->nodes = after.nodes - before.nodes;
+    stats->tris = after.tris - before.tris;
+    stats->shadow_rays = after.shadowRays - before.shadowRays;
+    stats->shadow_nodes = after.nodesS - before.nodesS;
+    stats->shadow_tris = after.trisS - before.trisS;
+    float ph[kPhN] = {0};
+    for (size_t i = 1; i < r->evs.size(); i++) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, r->evs[i - 1].second, r->evs[i].second);
+      ph[r->evs[i].first] += ms;
+    }
+    if (r->evs.size() > 1) cudaEventElapsedTime(&stats->ms_total, r->evs.front().second, r->evs.back().second);
+    stats->ms_light = ph[kPhLight];
+    stats->ms_trace = ph[kPhTrace];
+    stats->ms_shade = ph[kPhShade];
+    stats->ms_shadow = ph[kPhShadow];
+    stats->ms_filter = ph[kPhFilter];
+    stats->ms_adapt = ph[kPhAdapt];
+    if (after.errFlags) return fail(GBPT_ERR_BOUNDS, "device bounds check tripped (light cache)");
+  }
+  return GBPT_OK;
+}
+
+struct AttrDef {
+  const char* name;
+  int kind;  // 0 float, 1 uint
+  size_t off;
+};
+// reference attribute names first (src/cudaRTBDPTStreamAdapBilatAtomic.cu:48-60)
+const AttrDef kAttrs[] = {
+    {"Desired Max Sampling", 1, offsetof(gbpt_params, desired_n)},
+    {"Filter Color EuD", 0, offsetof(gbpt_params, filter_color_eud)},
+    {"Filter Pos EuD", 0, offsetof(gbpt_params, filter_pos_eud)},
+    {"Filter Norm EuD", 0, offsetof(gbpt_params, filter_norm_eud)},
+    {"Filter Diff EuD", 0, offsetof(gbpt_params, filter_diff_eud)},
+    {"Filter Radius", 1, offsetof(gbpt_params, filter_radius)},
+    {"Filter Diffuse Flag", 1, offsetof(gbpt_params, filter_diffuse)},
+    {"Eye Depth Max", 1, offsetof(gbpt_params, eye_depth_max)},
+    {"Light Depth Max", 1, offsetof(gbpt_params, light_depth_max)},
+    {"Light Paths", 1, offsetof(gbpt_params, light_paths)},
+    {"Light Pass Every", 1, offsetof(gbpt_params, light_every)},
+    {"Warmup Frames", 1, offsetof(gbpt_params, warmup_frames)},
+    {"Filter Sigma Spatial", 0, offsetof(gbpt_params, filter_sigma_spatial)},
+    {"Seed", 1, offsetof(gbpt_params, seed)},
+};
+constexpr uint32_t kAttrN = sizeof(kAttrs) / sizeof(kAttrs[0]);
+
+}  // namespace
+
+extern "C" {
+
+const char* gbpt_last_error_string(void) { return g_err.c_str(); }
+
+gbpt_status gbpt_device_check(int32_t* ok) {
+  if (!ok) return fail(GBPT_ERR_INVALID_ARG, "ok is NULL");
+  *ok = 0;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return fail(GBPT_ERR_NO_DEVICE, "no CUDA device");
+  float x = 1.f, y = 0.f;
+  float* d = nullptr;
+  if (cudaMalloc(&d, 8) != cudaSuccess) return fail(GBPT_ERR_NO_DEVICE, "cudaMalloc failed");
+  cudaMemcpy(d, &x, 4, cudaMemcpyHostToDevice);
+  e = launch_fmath(4, d, 1, d + 1, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(&y, d + 1, 4, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(GBPT_ERR_NO_DEVICE, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+  *ok = (y == 1.f) ? 1 : 0;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_params_default(gbpt_params* p) {
+  if (!p) return fail(GBPT_ERR_INVALID_ARG, "params is NULL");
+  std::memset(p, 0, sizeof(*p));
+  p->seed = 1234;
+  p->eye_depth_max = 5;
+  p->light_depth_max = 5;
+  p->light_paths = 128;
+  p->light_every = 3;
+  p->warmup_frames = 5;
+  p->desired_n = 5;
+  p->filter_color_eud = 50.f;
+  p->filter_pos_eud = 1.f;
+  p->filter_norm_eud = 0.25f;
+  p->filter_diff_eud = 0.1f;
+  p->filter_radius = 5;
+  p->filter_diffuse = 0;
+  p->filter_sigma_spatial = 0.f;
+  p->request_id = 0;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_scene_create(const gbpt_vertex* verts, uint32_t nv, const gbpt_triangle* tris, uint32_t nt,
+                              const gbpt_material* mats, uint32_t nm, gbpt_scene** out) {
+  if (!out) return fail(GBPT_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  if ((nv && !verts) || (nt && !tris) || (nm && !mats)) return fail(GBPT_ERR_INVALID_ARG, "NULL array");
+  for (uint32_t i = 0; i < nt; i++) {
+    if (tris[i].v0 >= nv || tris[i].v1 >= nv || tris[i].v2 >= nv)
+      return fail(GBPT_ERR_INVALID_ARG, "triangle " + std::to_string(i) + " has a vertex index out of range");
+    if (tris[i].mat >= nm)
+      return fail(GBPT_ERR_INVALID_ARG, "triangle " + std::to_string(i) + " has a material index out of range");
+  }
+  for (uint32_t i = 0; i < nv; i++)
+    for (int k = 0; k < 3; k++)
+      if (!std::isfinite(verts[i].pos[k]))
+        return fail(GBPT_ERR_INVALID_ARG, "vertex " + std::to_string(i) + " has a non-finite position");
+  gbpt_scene* s = new (std::nothrow) gbpt_scene();
+  if (!s) return fail(GBPT_ERR_OOM, "host allocation failed");
+  s->verts.assign(verts, verts + nv);
+  s->tris.assign(tris, tris + nt);
+  s->mats.assign(mats, mats + nm);
+  *out = s;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_scene_destroy(gbpt_scene* s) {
+  delete s;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_scene_build_bvh(gbpt_scene* s, uint32_t max_depth, uint32_t threads, double* build_seconds) {
+  if (!s) return fail(GBPT_ERR_INVALID_ARG, "scene is NULL");
+  if (s->tris.empty()) return fail(GBPT_ERR_STATE, "scene has no triangles");
+  if (max_depth == 0) max_depth = 32;
+  if (threads == 0) threads = std::max(1u, std::thread::hardware_concurrency());
+  auto t0 = std::chrono::steady_clock::now();
+  if (!build_bvh(s->verts.data(), s->tris.data(), (uint32_t)s->tris.size(), max_depth, threads, &s->bvh))
+    return fail(GBPT_ERR_STATE, "BVH compaction failed");
+  s->trisOrdered.resize(s->tris.size());
+  for (size_t i = 0; i < s->tris.size(); i++) s->trisOrdered[i] = s->tris[s->bvh.order[i]];
+  auto t1 = std::chrono::steady_clock::now();
+  if (build_seconds) *build_seconds = std::chrono::duration<double>(t1 - t0).count();
+  scan_lights(s);
+  s->free_dev();  // uploaded on first use (the reference uploads lazily in Render, :830-838)
+  s->uploaded = false;
+  s->built = true;
+  s->version = next_version();
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_scene_update_materials(gbpt_scene* s, const gbpt_material* mats, uint32_t nm) {
+  if (!s || !mats) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  if (nm != s->mats.size()) return fail(GBPT_ERR_INVALID_ARG, "material count differs from the scene's");
+  s->mats.assign(mats, mats + nm);
+  if (!s->built) return GBPT_OK;
+  scan_lights(s);
+  s->version = next_version();  // progressive accumulation restarts (src/cudaRTBDPTStream.cu:845-850)
+  if (!s->uploaded) return GBPT_OK;
+  std::vector<float4> m = pack_materials(s->mats);
+  CK(cudaMemcpy(s->dMats, m.data(), m.size() * 16, cudaMemcpyHostToDevice));
+  dfree(s->dLight);
+  CK(dalloc(&s->dLight, s->lightTri.size()));
+  if (!s->lightTri.empty())
+    CK(cudaMemcpy(s->dLight, s->lightTri.data(), s->lightTri.size() * 4, cudaMemcpyHostToDevice));
+  s->dev.lightTri = s->dLight;
+  s->dev.lightN = (uint32_t)s->lightTri.size();
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_scene_bvh_info(const gbpt_scene* s, uint32_t* node_count, uint32_t* tri_count,
+                                uint32_t* light_count) {
+  if (!s) return fail(GBPT_ERR_INVALID_ARG, "scene is NULL");
+  if (node_count) *node_count = s->built ? s->bvh.nodeN : 0;
+  if (tri_count) *tri_count = (uint32_t)s->tris.size();
+  if (light_count) *light_count = (uint32_t)s->lightTri.size();
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_scene_bvh_export(const gbpt_scene* s, float* bounds, uint32_t* off_or_tstn, uint32_t* tri_order) {
+  if (!s) return fail(GBPT_ERR_INVALID_ARG, "scene is NULL");
+  if (!s->built) return fail(GBPT_ERR_STATE, "scene has no BVH");
+  if (bounds) std::memcpy(bounds, s->bvh.bounds.data(), s->bvh.bounds.size() * 4);
+  if (off_or_tstn) std::memcpy(off_or_tstn, s->bvh.offOrTSTN.data(), s->bvh.offOrTSTN.size() * 4);
+  if (tri_order) std::memcpy(tri_order, s->bvh.order.data(), s->bvh.order.size() * 4);
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_trace_rays(gbpt_scene* s, const float* rays, uint32_t n, float max_dist, float eps, int32_t cullback,
+                            float* t, int32_t* tri, float* w, float* u, float* v, uint32_t* nodes,
+                            uint32_t* tris_tested, int32_t is_device) {
+  if (!s || !rays || !t || !tri || !w || !u || !v) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  gbpt_status up = ensure_uploaded(s);
+  if (up != GBPT_OK) return up;
+  if (n == 0) return GBPT_OK;
+  const bool counts = nodes && tris_tested;
+  if (is_device) {
+    CK(launch_trace_rays(s->dev, rays, n, max_dist, eps, cullback, t, tri, w, u, v, counts ? nodes : nullptr,
+                         counts ? tris_tested : nullptr, nullptr));
+    CK(cudaDeviceSynchronize());
+    return GBPT_OK;
+  }
+  float *dr = nullptr, *dt = nullptr, *dw = nullptr, *du = nullptr, *dv = nullptr;
+  int32_t* di = nullptr;
+  uint32_t *dn = nullptr, *dq = nullptr;
+  gbpt_status st = GBPT_OK;
+  auto cleanup = [&]() {
+    dfree(dr); dfree(dt); dfree(dw); dfree(du); dfree(dv); dfree(di); dfree(dn); dfree(dq);
+  };
+  do {
+    if (dalloc(&dr, (size_t)n * 6) || dalloc(&dt, n) || dalloc(&dw, n) || dalloc(&du, n) || dalloc(&dv, n) ||
+        dalloc(&di, n) || dalloc(&dn, n) || dalloc(&dq, n)) {
+      st = fail(GBPT_ERR_OOM, "device allocation for rays failed");
+      break;
+    }
+    cudaError_t e = cudaMemcpy(dr, rays, (size_t)n * 24, cudaMemcpyHostToDevice);
+    if (!e) e = launch_trace_rays(s->dev, dr, n, max_dist, eps, cullback, dt, di, dw, du, dv, counts ? dn : nullptr,
+                                  counts ? dq : nullptr, nullptr);
+    if (!e) e = cudaMemcpy(t, dt, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (!e) e = cudaMemcpy(tri, di, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (!e) e = cudaMemcpy(w, dw, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (!e) e = cudaMemcpy(u, du, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (!e) e = cudaMemcpy(v, dv, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (!e && counts) e = cudaMemcpy(nodes, dn, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (!e && counts) e = cudaMemcpy(tris_tested, dq, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (e) st = fail(GBPT_ERR_CUDA, std::string("trace_rays: ") + cudaGetErrorString(e));
+  } while (0);
+  cleanup();
+  return st;
+}
+
+gbpt_status gbpt_renderer_create(uint32_t width, uint32_t height, int32_t mode, const gbpt_params* params,
+                                 gbpt_renderer** out) {
+  if (!out) return fail(GBPT_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  if (width == 0 || height == 0 || (uint64_t)width * height > (1ull << 26))
+    return fail(GBPT_ERR_INVALID_ARG, "image size must be 1..2^26 pixels");
+  if (mode != GBPT_MODE_BDPT_SC && mode != GBPT_MODE_BDPT_SC_ADAP_BILAT)
+    return fail(GBPT_ERR_INVALID_ARG, "unknown renderer mode");
+  gbpt_params p;
+  if (params) {
+    gbpt_status st = check_params(params);
+    if (st != GBPT_OK) return st;
+    p = *params;
+  } else {
+    gbpt_params_default(&p);
+  }
+  gbpt_renderer* r = new (std::nothrow) gbpt_renderer();
+  if (!r) return fail(GBPT_ERR_OOM, "host allocation failed");
+  r->W = width;
+  r->H = height;
+  r->mode = mode;
+  r->p = p;
+  cudaError_t e = cudaStreamCreateWithFlags(&r->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete r;
+    return fail(GBPT_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+  }
+  *out = r;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_renderer_destroy(gbpt_renderer* r) {
+  delete r;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_set_mode(gbpt_renderer* r, int32_t mode) {
+  if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
+  if (mode != GBPT_MODE_BDPT_SC && mode != GBPT_MODE_BDPT_SC_ADAP_BILAT)
+    return fail(GBPT_ERR_INVALID_ARG, "unknown renderer mode");
+  if (mode != r->mode) {
+    r->mode = mode;
+    r->started = false;  // RTRenderer::SetRendererMode starts the new renderer from scratch
+  }
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_set_params(gbpt_renderer* r, const gbpt_params* params) {
+  if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
+  gbpt_status st = check_params(params);
+  if (st != GBPT_OK) return st;
+  bool realloc = params->light_paths * (1 + params->light_depth_max) > r->rb.cacheCap;
+  if (realloc && r->alloc) {
+    cudaStreamSynchronize(r->st);
+    r->free_dev();
+  }
+  r->p = *params;
+  r->started = false;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_get_params(const gbpt_renderer* r, gbpt_params* params) {
+  if (!r || !params) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  *params = r->p;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_render(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, float* out_rgb,
+                        int32_t out_is_device, gbpt_stats* stats) {
+  gbpt_status st = render_impl(r, s, cam, 1, out_rgb, out_is_device, stats);
+  if (st != GBPT_OK || out_rgb == nullptr || out_is_device) return st;
+  std::memcpy(r->hostResult.data(), out_rgb, r->hostResult.size() * 4);
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_render_frames(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, uint32_t frames,
+                               gbpt_stats* stats) {
+  return render_impl(r, s, cam, frames, nullptr, 0, stats);
+}
+
+const float* gbpt_result(gbpt_renderer* r) {
+  if (!r || !r->alloc) return nullptr;
+  if (cudaMemcpy(r->hostResult.data(), r->result, r->hostResult.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return nullptr;
+  return r->hostResult.data();
+}
+
+gbpt_status gbpt_read_buffer(gbpt_renderer* r, int32_t which, void* dst, size_t bytes, int32_t dst_is_device) {
+  if (!r || !dst) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  if (!r->alloc) return fail(GBPT_ERR_STATE, "renderer has not rendered yet");
+  const size_t np = (size_t)r->W * r->H;
+  const void* src = nullptr;
+  size_t need = np * 12;
+  switch (which) {
+    case 0: src = r->result; break;
+    case 1: src = r->gpos; break;
+    case 2: src = r->gnorm; break;
+    case 3: src = r->gdiff; break;
+    case 4: src = r->ab.filtered; break;
+    case 5: src = r->ab.err; need = np * 4; break;
+    case 6: src = r->sampleN; need = np * 4; break;
+    case 7: {  // light-vertex cache in the 21-float layout of the reference's LightVertex
+      DevCounters c{};
+      gbpt_status st = read_ctr(r, &c);
+      if (st != GBPT_OK) return st;
+      need = (size_t)c.cacheSize * 21 * 4;
+      if (bytes < need) return fail(GBPT_ERR_INVALID_ARG, "destination too small");
+      std::vector<float4> raw((size_t)c.cacheSize * 6);
+      if (c.cacheSize) CK(cudaMemcpy(raw.data(), r->rb.cache, raw.size() * 16, cudaMemcpyDeviceToHost));
+      std::vector<float> o((size_t)c.cacheSize * 21);
+      for (uint32_t i = 0; i < c.cacheSize; i++) {
+        const float4* q = &raw[(size_t)i * 6];
+        float* d = &o[(size_t)i * 21];
+        const float4* fields[6] = {&q[0], &q[1], &q[2], &q[3], &q[4], &q[5]};
+        for (int f = 0; f < 6; f++) {
+          d[f * 3] = fields[f]->x;
+          d[f * 3 + 1] = fields[f]->y;
+          d[f * 3 + 2] = fields[f]->z;
+        }
+        d[18] = q[0].w;  // specular
+        d[19] = q[1].w;  // metallic
+        d[20] = q[2].w;  // roughness
+      }
+      CK(cudaMemcpy(dst, o.data(), need, dst_is_device ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost));
+      return GBPT_OK;
+    }
+    default: return fail(GBPT_ERR_INVALID_ARG, "unknown buffer id");
+  }
+  if (bytes < need) return fail(GBPT_ERR_INVALID_ARG, "destination too small");
+  CK(cudaStreamSynchronize(r->st));
+  CK(cudaMemcpy(dst, src, need, dst_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_reset(gbpt_renderer* r) {
+  if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
+  r->started = false;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_clean(gbpt_renderer* r) {
+  if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
+  cudaStreamSynchronize(r->st);
+  r->free_dev();
+  r->started = false;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_set_counting(gbpt_renderer* r, int32_t on) {
+  if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
+  r->counting = on != 0;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_attr_count(const gbpt_renderer* r, uint32_t* n) {
+  if (!r || !n) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  *n = kAttrN + 1;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_attr_name(const gbpt_renderer* r, uint32_t index, char* name, size_t cap) {
+  if (!r || !name || cap == 0) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  const char* nm = nullptr;
+  if (index < kAttrN)
+    nm = kAttrs[index].name;
+  else if (index == kAttrN)
+    nm = "Debug Mode";
+  else
+    return fail(GBPT_ERR_INVALID_ARG, "attribute index out of range");
+  std::strncpy(name, nm, cap - 1);
+  name[cap - 1] = 0;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_attr_get(const gbpt_renderer* r, const char* name, float* value) {
+  if (!r || !name || !value) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  if (std::strcmp(name, "Debug Mode") == 0) {
+    *value = r->debugMode;
+    return GBPT_OK;
+  }
+  for (uint32_t i = 0; i < kAttrN; i++)
+    if (std::strcmp(name, kAttrs[i].name) == 0) {
+      const char* base = (const char*)&r->p;
+      if (kAttrs[i].kind == 0)
+        std::memcpy(value, base + kAttrs[i].off, 4);
+      else {
+        uint32_t u;
+        std::memcpy(&u, base + kAttrs[i].off, 4);
+        *value = (float)u;
+      }
+      return GBPT_OK;
+    }
+  return fail(GBPT_ERR_INVALID_ARG, std::string("unknown attribute '") + name + "'");
+}
+
+gbpt_status gbpt_attr_set(gbpt_renderer* r, const char* name, float value) {
+  if (!r || !name) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  if (std::strcmp(name, "Debug Mode") == 0) {
+    if (value != 0.f && value != 4.f) return fail(GBPT_ERR_INVALID_ARG, "Debug Mode supports 0 (None) and 4 (Filtered)");
+    r->debugMode = value;
+    return GBPT_OK;
+  }
+  for (uint32_t i = 0; i < kAttrN; i++)
+    if (std::strcmp(name, kAttrs[i].name) == 0) {
+      gbpt_params p = r->p;
+      char* base = (char*)&p;
+      if (kAttrs[i].kind == 0) {
+        std::memcpy(base + kAttrs[i].off, &value, 4);
+      } else {
+        if (!(value >= 0.f) || value > 4294967295.f) return fail(GBPT_ERR_INVALID_ARG, "value out of range");
+        uint32_t u = (uint32_t)value;
+        std::memcpy(base + kAttrs[i].off, &u, 4);
+      }
+      return gbpt_set_params(r, &p);
+    }
+  return fail(GBPT_ERR_INVALID_ARG, std::string("unknown attribute '") + name + "'");
+}
+
+gbpt_status gbpt_gaussian_table(float delta, uint32_t radius, float* g) {
+  if (!g) return fail(GBPT_ERR_INVALID_ARG, "g is NULL");
+  if (radius > 31) return fail(GBPT_ERR_INVALID_ARG, "radius must be <= 31");
+  gaussian_table_host(delta, radius, g);
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_bilateral(const float* color, const float* pos, const float* norm, const float* emit,
+                           uint32_t width, uint32_t height, float color_eud, float pos_eud, float norm_eud,
+                           float emit_eud, uint32_t radius, const float* g, float* out, int32_t is_device) {
+  if (!color || !pos || !norm || !g || !out) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  if (radius > 31 || width == 0 || height == 0) return fail(GBPT_ERR_INVALID_ARG, "bad size or radius");
+  const size_t n = (size_t)width * height * 3;
+  float* dg = nullptr;
+  CK(dalloc(&dg, 2 * radius + 1));
+  CK(cudaMemcpy(dg, g, (2 * radius + 1) * 4, cudaMemcpyHostToDevice));
+  gbpt_status st = GBPT_OK;
+  if (is_device) {
+    cudaError_t e = launch_bilateral(color, pos, norm, emit, width, height, color_eud, pos_eud, norm_eud, emit_eud,
+                                     radius, dg, out, nullptr);
+    if (!e) e = cudaDeviceSynchronize();
+    if (e) st = fail(GBPT_ERR_CUDA, std::string("bilateral: ") + cudaGetErrorString(e));
+  } else {
+    float* d[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    const float* src[4] = {color, pos, norm, emit};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 5 && !e; k++) {
+      if (k < 4 && !src[k]) continue;
+      e = dalloc(&d[k], n);
+      if (!e && k < 4) e = cudaMemcpy(d[k], src[k], n * 4, cudaMemcpyHostToDevice);
+    }
+    if (!e)
+      e = launch_bilateral(d[0], d[1], d[2], d[3], width, height, color_eud, pos_eud, norm_eud, emit_eud, radius, dg,
+                           d[4], nullptr);
+    if (!e) e = cudaMemcpy(out, d[4], n * 4, cudaMemcpyDeviceToHost);
+    for (int k = 0; k < 5; k++) dfree(d[k]);
+    if (e) st = fail(GBPT_ERR_CUDA, std::string("bilateral: ") + cudaGetErrorString(e));
+  }
+  dfree(dg);
+  return st;
+}
+
+gbpt_status gbpt_fmath(int32_t which, const float* x, uint32_t n, float* out) {
+  if (!x || !out || which < 0 || which > 4) return fail(GBPT_ERR_INVALID_ARG, "bad argument");
+  if (n == 0) return GBPT_OK;
+  float *dx = nullptr, *dy = nullptr;
+  CK(dalloc(&dx, n));
+  CK(dalloc(&dy, n));
+  cudaError_t e = cudaMemcpy(dx, x, (size_t)n * 4, cudaMemcpyHostToDevice);
+  if (!e) e = launch_fmath(which, dx, n, dy, nullptr);
+  if (!e) e = cudaMemcpy(out, dy, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  dfree(dx);
+  dfree(dy);
+  if (e) return fail(GBPT_ERR_CUDA, std::string("fmath: ") + cudaGetErrorString(e));
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_philox(const uint32_t* ctr, uint32_t n, uint32_t k0, uint32_t k1, uint32_t* out) {
+  if (!ctr || !out) return fail(GBPT_ERR_INVALID_ARG, "bad argument");
+  if (n == 0) return GBPT_OK;
+  uint32_t *dc = nullptr, *dout = nullptr;
+  CK(dalloc(&dc, (size_t)n * 4));
+  CK(dalloc(&dout, (size_t)n * 4));
+  cudaError_t e = cudaMemcpy(dc, ctr, (size_t)n * 16, cudaMemcpyHostToDevice);
+  if (!e) e = launch_philox(dc, n, k0, k1, dout, nullptr);
+  if (!e) e = cudaMemcpy(out, dout, (size_t)n * 16, cudaMemcpyDeviceToHost);
+  dfree(dc);
+  dfree(dout);
+  if (e) return fail(GBPT_ERR_CUDA, std::string("philox: ") + cudaGetErrorString(e));
+  return GBPT_OK;
+}
+
+}  // extern "C"

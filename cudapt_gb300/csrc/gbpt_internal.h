@@ -1,0 +1,27 @@
+// Internal declarations shared by the translation units of libgbpt.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/gbpt.h"
+
+namespace gbpt {
+
+// CompactBVH in host memory (include/bvhhelper.h:45-54) + CreateBVH's order.
+struct HostBVH {
+  uint32_t nodeN = 0;
+  std::vector<float> bounds;        // 6 per node
+  std::vector<uint32_t> offOrTSTN;  // 2 per node
+  std::vector<uint32_t> order;      // triangle order
+  uint32_t emptyChildren = 0;
+};
+
+bool build_bvh(const gbpt_vertex* verts, const gbpt_triangle* tris, uint32_t nt, uint32_t maxDepth, uint32_t threads,
+               HostBVH* out);
+
+// thread-local error text (gbpt_last_error_string)
+void set_error(const std::string& s);
+gbpt_status fail(gbpt_status st, const std::string& s);
+
+}  // namespace gbpt

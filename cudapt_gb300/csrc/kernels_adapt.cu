@@ -1,0 +1,426 @@
+// Adaptive sampling and bilateral-filter kernels for GB300 (sm_103a).
+//
+//   bilateral   bilaterial_posnorm_kernel / bilaterial_posnormemit_kernel
+//               (src/cudaBilateralFilter.cu:66-142), shared-memory tiles
+//   error       pt_calculateSquareError_kernel (src/cudaRTBDPTStreamAdapBilatAtomic.cu:1143-1156)
+//               fused with a per-block FP64 partial sum (replaces thrust::reduce, :1444)
+//   budget      pt_genAdapPathQueue_kernel (:817-842): floor(W*H * e_p / sum e)
+//               samples per pixel, laid out pixel-major by an exclusive scan
+//               (replaces the warp-aggregated atomic append, src/cudaRTCommon.cu:620-628)
+//   accumulate  pt_atomicApplyPathQueueResult_kernel + pt_accumTempResultToResult_kernel
+//               (:1041-1141): each pixel sums its own samples in sample order
+//               instead of float atomics, so the result does not depend on timing.
+#include <cuda_runtime.h>
+
+#include "gbpt_math.cuh"
+#include "launch.h"
+
+namespace gbpt {
+
+namespace {
+
+constexpr int kTile = 16;
+constexpr int kScanBlock = 1024;
+constexpr int kReduceBlock = 256;
+
+__device__ __forceinline__ float eucl(float ax, float ay, float az, float bx, float by, float bz, float c2) {
+  // src/cudaBilateralFilter.cu:26-33: exp(-|b-a|^2 / (2 d d)), c2 = (2*d)*d
+  float dx = bx - ax, dy = by - ay, dz = bz - az;
+  float mod = (dx * dx + dy * dy) + dz * dz;
+  return gb::exp_p(-mod / c2);
+}
+
+// Tap (x+j, y+i) with the reference's unsigned arithmetic: a coordinate left
+// of column 0 wraps to a huge value and min() sends it to the last column.
+__device__ __forceinline__ uint32_t wrapc(int g, uint32_t n) { return ((uint32_t)g < n) ? (uint32_t)g : n - 1; }
+
+// One 16x16 output tile; the (16+2r)^2 input window of every plane is
+// staged in shared memory (planes stored as float triples).
+template <bool kEmit>
+__global__ void __launch_bounds__(kTile* kTile) k_bilateral_tile(const float* __restrict__ color,
+                                                                  const float* __restrict__ pos,
+                                                                  const float* __restrict__ norm,
+                                                                  const float* __restrict__ emit, uint32_t W,
+                                                                  uint32_t H, float cc2, float pc2, float nc2,
+                                                                  float ec2, int r, const float* __restrict__ g,
+                                                                  float* __restrict__ out) {
+  extern __shared__ float sm[];
+  const int T = kTile + 2 * r;
+  const int planes = kEmit ? 4 : 3;
+  float* sg = sm;                      // 2r+1 gaussian weights
+  float* tile = sm + ((2 * r + 1 + 3) & ~3);
+  const int x0 = blockIdx.x * kTile - r, y0 = blockIdx.y * kTile - r;
+  const int tid = threadIdx.y * kTile + threadIdx.x;
+  for (int k = tid; k < 2 * r + 1; k += kTile * kTile) sg[k] = g[k];
+  for (int k = tid; k < T * T; k += kTile * kTile) {
+    int ty = k / T, tx = k - ty * T;
+    uint32_t gx = wrapc(x0 + tx, W), gy = wrapc(y0 + ty, H);
+    size_t src = 3 * ((size_t)gy * W + gx);
+    float* dst = tile + 3 * (size_t)k * planes;
+    dst[0] = color[src]; dst[1] = color[src + 1]; dst[2] = color[src + 2];
+    dst[3] = pos[src];   dst[4] = pos[src + 1];   dst[5] = pos[src + 2];
+    dst[6] = norm[src];  dst[7] = norm[src + 1];  dst[8] = norm[src + 2];
+    if (kEmit) { dst[9] = emit[src]; dst[10] = emit[src + 1]; dst[11] = emit[src + 2]; }
+  }
+  __syncthreads();
+  const uint32_t x = blockIdx.x * kTile + threadIdx.x, y = blockIdx.y * kTile + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const float* cen = tile + 3 * (size_t)((threadIdx.y + r) * T + threadIdx.x + r) * planes;
+  float sum = 0.f, tx = 0.f, ty = 0.f, tz = 0.f;
+  for (int i = -r; i <= r; i++) {
+    const float gi = sg[i + r];
+    for (int j = -r; j <= r; j++) {
+      const float* q = tile + 3 * (size_t)((threadIdx.y + r + i) * T + threadIdx.x + r + j) * planes;
+      float f = gi * sg[j + r];
+      f = f * eucl(q[0], q[1], q[2], cen[0], cen[1], cen[2], cc2);
+      f = f * eucl(q[3], q[4], q[5], cen[3], cen[4], cen[5], pc2);
+      f = f * eucl(q[6], q[7], q[8], cen[6], cen[7], cen[8], nc2);
+      if (kEmit) f = f * eucl(q[9], q[10], q[11], cen[9], cen[10], cen[11], ec2);
+      tx = tx + f * q[0];
+      ty = ty + f * q[1];
+      tz = tz + f * q[2];
+      sum = sum + f;
+    }
+  }
+  float* o = out + 3 * ((size_t)y * W + x);
+  o[0] = tx / sum;
+  o[1] = ty / sum;
+  o[2] = tz / sum;
+}
+
+// Same arithmetic, reading global memory directly (large radii).
+template <bool kEmit>
+__global__ void k_bilateral_direct(const float* __restrict__ color, const float* __restrict__ pos,
+                                   const float* __restrict__ norm, const float* __restrict__ emit, uint32_t W,
+                                   uint32_t H, float cc2, float pc2, float nc2, float ec2, int r,
+                                   const float* __restrict__ g, float* __restrict__ out) {
+  const uint32_t x = blockIdx.x * kTile + threadIdx.x, y = blockIdx.y * kTile + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const size_t c = 3 * ((size_t)y * W + x);
+  float sum = 0.f, tx = 0.f, ty = 0.f, tz = 0.f;
+  for (int i = -r; i <= r; i++)
+    for (int j = -r; j <= r; j++) {
+      size_t q = 3 * ((size_t)wrapc((int)y + i, H) * W + wrapc((int)x + j, W));
+      float f = g[i + r] * g[j + r];
+      f = f * eucl(color[q], color[q + 1], color[q + 2], color[c], color[c + 1], color[c + 2], cc2);
+      f = f * eucl(pos[q], pos[q + 1], pos[q + 2], pos[c], pos[c + 1], pos[c + 2], pc2);
+      f = f * eucl(norm[q], norm[q + 1], norm[q + 2], norm[c], norm[c + 1], norm[c + 2], nc2);
+      if (kEmit) f = f * eucl(emit[q], emit[q + 1], emit[q + 2], emit[c], emit[c + 1], emit[c + 2], ec2);
+      tx = tx + f * color[q];
+      ty = ty + f * color[q + 1];
+      tz = tz + f * color[q + 2];
+      sum = sum + f;
+    }
+  out[c] = tx / sum;
+  out[c + 1] = ty / sum;
+  out[c + 2] = tz / sum;
+}
+
+// per-pixel error and per-block FP64 partial sums
+__global__ void __launch_bounds__(kReduceBlock) k_error(const float* __restrict__ filtered,
+                                                        const float* __restrict__ result,
+                                                        const uint32_t* __restrict__ sampleN, uint32_t np,
+                                                        uint32_t D, float* __restrict__ err,
+                                                        double* __restrict__ partial) {
+  __shared__ double ws[kReduceBlock / 32];
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (p < np) {
+    uint32_t sn = sampleN[p];
+    float rf = (float)D / (float)(D + sn);
+    if (D + sn < sn) rf = 0.f;
+    const float* a = filtered + 3 * (size_t)p;
+    const float* b = result + 3 * (size_t)p;
+    float d0 = a[0] - b[0], d1 = a[1] - b[1], d2 = a[2] - b[2];
+    float e = (rf * ((d0 * d0 + d1 * d1) + d2 * d2)) / 3.f;
+    err[p] = e;
+    v = (double)e;
+  }
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kReduceBlock / 32; w++) s += ws[w];
+    partial[blockIdx.x] = s;
+  }
+}
+
+__global__ void k_reduce_final(const double* __restrict__ partial, uint32_t n, DevCounters* ctr) {
+  __shared__ double ws[32];
+  double v = 0.0;
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) v += partial[i];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (uint32_t w = 0; w < (blockDim.x + 31) / 32; w++) s += ws[w];
+    ctr->errSum = s;
+  }
+}
+
+// counts and block-local exclusive scan
+__global__ void __launch_bounds__(kScanBlock) k_budget(const float* __restrict__ err, uint32_t np,
+                                                       const DevCounters* __restrict__ ctr, uint32_t* cnt,
+                                                       uint32_t* off, uint32_t* blockSum) {
+  __shared__ uint32_t ws[kScanBlock / 32];
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  const float sumF = (float)ctr->errSum;
+  uint32_t c = 0;
+  if (p < np) {
+    float ratio = err[p] / sumF;
+    float v = (float)np * ratio;
+    c = (v >= 1.f && v < 4294967040.f) ? (uint32_t)v : 0u;
+    cnt[p] = c;
+  }
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = c;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (uint32_t)o) incl += t;
+  }
+  if (lane == 31) ws[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t s = (lane < kScanBlock / 32) ? ws[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= (uint32_t)o) s += t;
+    }
+    if (lane < kScanBlock / 32) ws[lane] = s;
+  }
+  __syncthreads();
+  uint32_t before = (warp > 0) ? ws[warp - 1] : 0u;
+  if (p < np) off[p] = before + incl - c;
+  if (threadIdx.x == blockDim.x - 1) blockSum[blockIdx.x] = ws[kScanBlock / 32 - 1];
+}
+
+// exclusive scan of the block sums (one CTA; 64-bit running total)
+__global__ void k_scan_blocks(uint32_t* blockSum, uint32_t nb, uint32_t gen, DevCounters* ctr) {
+  __shared__ unsigned long long carry;
+  __shared__ uint32_t ws[32];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (uint32_t base = 0; base < nb; base += blockDim.x) {
+    uint32_t i = base + threadIdx.x;
+    uint32_t v = (i < nb) ? blockSum[i] : 0u;
+    uint32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += t;
+    }
+    if (lane == 31) ws[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t s = (lane < nw) ? ws[lane] : 0u;
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= (uint32_t)o) s += t;
+      }
+      if (lane < nw) ws[lane] = s;
+    }
+    __syncthreads();
+    unsigned long long c0 = carry;
+    unsigned long long ex = c0 + ((warp > 0) ? ws[warp - 1] : 0u) + incl - v;
+    if (i < nb) blockSum[i] = (uint32_t)(ex < gen ? ex : gen);
+    __syncthreads();
+    if (threadIdx.x == 0) carry = c0 + ws[nw - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    unsigned long long tot = carry < gen ? carry : gen;
+    ctr->wave[0] = (uint32_t)tot;
+    ctr->paths = (uint32_t)tot;
+  }
+}
+
+// global clamped offsets: off_c = min(prefix, gen), cnt_c = min(prefix+cnt, gen) - off_c
+__global__ void k_offsets(uint32_t* off, uint32_t* cnt, const uint32_t* blockSum, uint32_t np, uint32_t gen) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  unsigned long long pre = (unsigned long long)blockSum[p / kScanBlock] + off[p];
+  unsigned long long a = pre < gen ? pre : gen;
+  unsigned long long e = pre + cnt[p];
+  unsigned long long b = e < gen ? e : gen;
+  off[p] = (uint32_t)a;
+  cnt[p] = (uint32_t)(b - a);
+}
+
+// one camera path per budgeted sample; slot s belongs to the last pixel whose
+// offset is <= s (pixels without samples share their successor's offset).
+__global__ void k_gen_adapt(FrameArgs a, RenderBuffers b, const uint32_t* __restrict__ off,
+                            const uint32_t* __restrict__ cnt) {
+  using namespace gb;
+  const uint32_t total = b.ctr->wave[0];
+  const uint32_t np = a.width * a.height;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < total; s += stride) {
+    uint32_t lo = 0, hi = np;  // first index with off > s
+    while (lo < hi) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (off[mid] <= s)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    const uint32_t p = lo - 1;
+    const uint32_t k = s - off[p];
+    const uint32_t x = p % a.width, y = p / a.width;
+    float u[4];
+    draw4(a.key0, a.key1, p, a.frame, kCamera, 0, k, 0, u);
+    const float W = a.W, H = a.H, th = a.tanHalf;
+    float cu = ((((2.f * ((float)x + 0.5f)) / W) - 1.f) * th * W) / H;
+    float cv = (((2.f * ((float)y + 0.5f)) / H) - 1.f) * th;
+    float au = cu + ((u[0] - 0.5f) / H) * th;
+    float av = cv + ((u[1] - 0.5f) / H) * th;
+    f3 R = mk(a.camRight[0], a.camRight[1], a.camRight[2]);
+    f3 U = mk(a.camUp[0], a.camUp[1], a.camUp[2]);
+    f3 D = mk(a.camDir[0], a.camDir[1], a.camDir[2]);
+    f3 dir = normalize((R * au + U * av) + D);
+    Wave w = b.wave[0];
+    w.o[s] = make_float4(a.camPos[0], a.camPos[1], a.camPos[2], __uint_as_float(s));
+    w.d[s] = make_float4(dir.x, dir.y, dir.z, __uint_as_float(p));
+    w.thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
+    w.smp[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+    b.res[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+    b.slotPix[s] = p;
+    b.slotSmp[s] = k;
+    b.gbuf[3 * (size_t)s] = make_float4(0.f, 0.f, 0.f, 0.f);
+    b.gbuf[3 * (size_t)s + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    b.gbuf[3 * (size_t)s + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+// ordered per-pixel sums, then the running means
+__global__ void k_accum(FrameArgs a, RenderBuffers b, const uint32_t* __restrict__ off,
+                        const uint32_t* __restrict__ cnt, float* result, uint32_t* sampleN, float* gpos,
+                        float* gnorm, float* gdiff) {
+  const uint32_t np = a.width * a.height;
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  float tr[3] = {0.f, 0.f, 0.f}, tp[3] = {0.f, 0.f, 0.f}, tn[3] = {0.f, 0.f, 0.f}, td[3] = {0.f, 0.f, 0.f};
+  uint32_t tN = 0;
+  const uint32_t o = off[p], c = cnt[p];
+  for (uint32_t s = o; s < o + c; s++) {
+    float4 r = b.res[s];
+    if (isinf(r.x) || isinf(r.y) || isinf(r.z)) continue;
+    uint32_t n = __float_as_uint(r.w);
+    float fn = (float)n;
+    float4 g0 = b.gbuf[3 * (size_t)s], g1 = b.gbuf[3 * (size_t)s + 1], g2 = b.gbuf[3 * (size_t)s + 2];
+    tr[0] = tr[0] + r.x; tr[1] = tr[1] + r.y; tr[2] = tr[2] + r.z;
+    tp[0] = tp[0] + g0.x * fn; tp[1] = tp[1] + g0.y * fn; tp[2] = tp[2] + g0.z * fn;
+    tn[0] = tn[0] + g1.x * fn; tn[1] = tn[1] + g1.y * fn; tn[2] = tn[2] + g1.z * fn;
+    td[0] = td[0] + g2.x * fn; td[1] = td[1] + g2.y * fn; td[2] = td[2] + g2.z * fn;
+    tN += n;
+  }
+  float* q = result + 3 * (size_t)p;
+  float* P = gpos + 3 * (size_t)p;
+  float* Nn = gnorm + 3 * (size_t)p;
+  float* Dd = gdiff + 3 * (size_t)p;
+  uint32_t N = sampleN[p];
+  if (a.frame == 0) {
+    N = 0;
+    for (int k = 0; k < 3; k++) q[k] = P[k] = Nn[k] = Dd[k] = 0.f;
+  }
+  const uint32_t nn = tN + N;
+  if (nn > N) {
+    const float rInf = 1.f / (float)nn, oInf = (float)N * rInf;
+    for (int k = 0; k < 3; k++) {
+      q[k] = fmaxf(rInf * tr[k] + oInf * q[k], 0.f);
+      P[k] = rInf * tp[k] + oInf * P[k];
+      Nn[k] = rInf * tn[k] + oInf * Nn[k];
+      Dd[k] = rInf * td[k] + oInf * Dd[k];
+    }
+    N = nn;
+  }
+  sampleN[p] = N;
+}
+
+__global__ void k_fmath(int which, const float* x, uint32_t n, float* out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s, c, v = x[i], r = 0.f;
+  switch (which) {
+    case 0: gb::sincos_p(v, &s, &c); r = s; break;
+    case 1: gb::sincos_p(v, &s, &c); r = c; break;
+    case 2: r = gb::exp_p(v); break;
+    case 3: r = gb::sqrt_rd_(v); break;
+    case 4: r = gb::pow5(v); break;
+  }
+  out[i] = r;
+}
+
+__global__ void k_philox(const uint32_t* ctr, uint32_t n, uint32_t k0, uint32_t k1, uint32_t* out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  gb::u4 r = gb::philox(gb::u4{ctr[4 * i], ctr[4 * i + 1], ctr[4 * i + 2], ctr[4 * i + 3]}, k0, k1);
+  out[4 * i] = r.a;
+  out[4 * i + 1] = r.b;
+  out[4 * i + 2] = r.c;
+  out[4 * i + 3] = r.d;
+}
+
+}  // namespace
+
+uint32_t adapt_scan_blocks(uint32_t np) { return (np + kScanBlock - 1) / kScanBlock; }
+uint32_t adapt_reduce_blocks(uint32_t np) { return (np + kReduceBlock - 1) / kReduceBlock; }
+
+cudaError_t launch_bilateral(const float* color, const float* pos, const float* norm, const float* emit, uint32_t W,
+                             uint32_t H, float ceud, float peud, float neud, float eeud, uint32_t radius,
+                             const float* g, float* out, cudaStream_t st) {
+  const float cc2 = 2.f * ceud * ceud, pc2 = 2.f * peud * peud, nc2 = 2.f * neud * neud, ec2 = 2.f * eeud * eeud;
+  dim3 grid((W + kTile - 1) / kTile, (H + kTile - 1) / kTile), block(kTile, kTile);
+  const int r = (int)radius;
+  const int T = kTile + 2 * r;
+  const int planes = emit ? 4 : 3;
+  size_t smem = (size_t)(((2 * r + 1 + 3) & ~3) + 3 * T * T * planes) * sizeof(float);
+  if (smem <= 200 * 1024) {
+    if (emit) {
+      cudaFuncSetAttribute(k_bilateral_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_bilateral_tile<true><<<grid, block, smem, st>>>(color, pos, norm, emit, W, H, cc2, pc2, nc2, ec2, r, g, out);
+    } else {
+      cudaFuncSetAttribute(k_bilateral_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_bilateral_tile<false><<<grid, block, smem, st>>>(color, pos, norm, emit, W, H, cc2, pc2, nc2, ec2, r, g,
+                                                          out);
+    }
+  } else if (emit) {
+    k_bilateral_direct<true><<<grid, block, 0, st>>>(color, pos, norm, emit, W, H, cc2, pc2, nc2, ec2, r, g, out);
+  } else {
+    k_bilateral_direct<false><<<grid, block, 0, st>>>(color, pos, norm, emit, W, H, cc2, pc2, nc2, ec2, r, g, out);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adapt_budget(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab,
+                                const float* result, const uint32_t* sampleN, uint32_t desired, cudaStream_t st) {
+  const uint32_t np = a.width * a.height;
+  const uint32_t nr = adapt_reduce_blocks(np), ns = adapt_scan_blocks(np);
+  k_error<<<nr, kReduceBlock, 0, st>>>(ab.filtered, result, sampleN, np, desired, ab.err, ab.partial);
+  k_reduce_final<<<1, 1024, 0, st>>>(ab.partial, nr, b.ctr);
+  k_budget<<<ns, kScanBlock, 0, st>>>(ab.err, np, b.ctr, ab.cnt, ab.off, ab.blockSum);
+  k_scan_blocks<<<1, 1024, 0, st>>>(ab.blockSum, ns, np, b.ctr);
+  k_offsets<<<(np + 255) / 256, 256, 0, st>>>(ab.off, ab.cnt, ab.blockSum, np, np);
+  k_gen_adapt<<<sm_count() * 8, 256, 0, st>>>(a, b, ab.off, ab.cnt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adapt_accum(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab, float* result,
+                               uint32_t* sampleN, float* gpos, float* gnorm, float* gdiff, cudaStream_t st) {
+  const uint32_t np = a.width * a.height;
+  k_accum<<<(np + 255) / 256, 256, 0, st>>>(a, b, ab.off, ab.cnt, result, sampleN, gpos, gnorm, gdiff);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fmath(int which, const float* x, uint32_t n, float* out, cudaStream_t st) {
+  if (n) k_fmath<<<(n + 255) / 256, 256, 0, st>>>(which, x, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_philox(const uint32_t* ctr, uint32_t n, uint32_t k0, uint32_t k1, uint32_t* out, cudaStream_t st) {
+  if (n) k_philox<<<(n + 255) / 256, 256, 0, st>>>(ctr, n, k0, k1, out);
+  return cudaGetLastError();
+}
+
+}  // namespace gbpt

@@ -1,0 +1,649 @@
+// Wavefront BDPT kernels for GB300 (sm_103a).
+//
+// One frame of the reference's streaming BDPT (src/cudaRTBDPTStream.cu:816-951)
+// runs as a fixed sequence of launches with no host round trip:
+//
+//   light pass (1 CTA)          pt_genLightPathQueue_kernel + pt_traceLight_kernel
+//                               loop with stable compaction (:875-906)
+//   camera                      pt_genPathQueue_kernel (:619-640)
+//   per bounce d:
+//     trace  (closest hit)      the TracePrimitive half of pt_traceSample_kernel
+//     shade                     the rest of pt_traceSample_kernel (:365-543);
+//                               survivors are appended to the other wave
+//                               buffer with one atomic per warp (replaces
+//                               thrust::remove_if, :930), connection requests
+//                               likewise (replaces thrust::copy_if, :934)
+//     shadow (any hit)          the visibility test of GetLightFromRandLightVertices
+//                               (:665-700) and the accumulate of
+//                               pt_connectEyeLightPath_kernel (:703-723)
+//   apply                       pt_applyPathQueueResult_kernel (:741-778)
+//
+// Queue lengths live in device memory (DevCounters) and every kernel runs a
+// grid-stride loop over them, so the host never waits on a count.
+#include <cuda_runtime.h>
+
+#include "launch.h"
+#include "shade.cuh"
+#include "trace.cuh"
+
+namespace gbpt {
+
+using gb::f3;
+using gb::mk;
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ f3 ld3(float4 v) { return mk(v.x, v.y, v.z); }
+__device__ __forceinline__ float4 st4(f3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
+__device__ __forceinline__ float4 st4u(f3 v, uint32_t w) { return make_float4(v.x, v.y, v.z, __uint_as_float(w)); }
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+struct Mat {
+  f3 diff, emis;
+  float trans, spec, metal, rough;
+};
+__device__ __forceinline__ Mat load_mat(const DevScene& S, uint32_t id) {
+  float4 a = __ldg(S.mats + 3 * (size_t)id), b = __ldg(S.mats + 3 * (size_t)id + 1),
+         c = __ldg(S.mats + 3 * (size_t)id + 2);
+  Mat m;
+  m.diff = ld3(a);
+  m.trans = a.w;
+  m.emis = ld3(b);
+  m.spec = b.w;
+  m.metal = c.x;
+  m.rough = c.y;
+  return m;
+}
+
+// interpolated normal, position and material id of a triangle at (w,u,v):
+// ((x0*w) + (x1*u)) + (x2*v) as the reference's float3 operators.
+struct Surf {
+  f3 norm, pos;
+  uint32_t mat;
+};
+__device__ __forceinline__ Surf load_surf(const DevScene& S, uint32_t tri, float w, float u, float v, bool wantPos) {
+  const float4* r = S.shade + 5 * (size_t)tri;
+  float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), d = __ldg(r + 3);
+  Surf s;
+  s.norm = (ld3(a) * w + ld3(b) * u) + ld3(c) * v;
+  s.mat = __float_as_uint(d.w);
+  if (wantPos) {
+    float4 e = __ldg(r + 4);
+    s.pos = (mk(a.w, b.w, c.w) * w + ld3(d) * u) + ld3(e) * v;
+  } else {
+    s.pos = mk(0.f, 0.f, 0.f);
+  }
+  return s;
+}
+
+enum : uint32_t { kTypeEye = 0, kTypeDiff = 1, kTypeSpec = 2, kTypeLight = 3 };
+
+// The bounce decision shared by eye and light paths (reflect / transmit /
+// diffuse, src/cudaRTBDPTStream.cu:400-493 and :223-323).
+struct Bounce {
+  f3 nl, nOrig, nDir, lmt, F;
+  uint32_t type;
+};
+__device__ __forceinline__ void sample_bounce(f3 orig, f3 dir, float dist, f3 norm, const Mat& m, const float* u,
+                                              bool specPush, Bounce& B) {
+  using namespace gb;
+  B.nl = dot(norm, dir) < 0.f ? norm : -1.f * norm;
+  const f3 nl = B.nl;
+  f3 hDir = ggx_sample(u[0], u[1], m.rough, nl);
+  f3 ndir = -1.f * dir;
+  float voH = dot(ndir, hDir);
+  f3 f0 = vlerp(kF0Spec * mk(m.spec, m.spec, m.spec), m.diff, m.metal);
+  f3 F = f_schlick(f0, voH);
+  B.F = F;
+  float reflProb = lerp(length(F), 1.0f, m.metal);
+  float refrProb = m.trans;
+  f3 reflDir = mk(0.f, 0.f, 0.f), refrDir = reflDir;
+  if (refrProb > 0.f) {
+    bool into = dot(nl, norm) > 0.f;
+    float nt = m.spec * 0.8f + 1.f;
+    float nnt = into ? 1.0f / nt : nt / 1.0f;
+    float ddn = dot(hDir, dir);
+    float cos2t = 1.f - (nnt * nnt) * (1.f - ddn * ddn);
+    refrDir = normalize(dir * nnt - hDir * (ddn * nnt + sqrtf(cos2t)));
+  }
+  if (reflProb > 0.f) {
+    reflDir = normalize(dir - (hDir * 2.f) * dot(hDir, dir));
+    if (dot(reflDir, nl) < 0.f) reflProb = 0.f;
+  }
+  if (prob_rand(reflProb, u[2])) {
+    B.nOrig = orig + (dist - kBias) * dir;
+    if (specPush) B.nOrig = B.nOrig + reflDir * kBias;
+    B.nDir = reflDir;
+    float VoH = dot(ndir, hDir), NoV = dot(nl, ndir), NoH = dot(nl, hDir), NoL = dot(nl, reflDir);
+    float G = vis_smith(m.rough, NoV, NoL);
+    B.lmt = ((F * G) * VoH) / ((NoV * NoH) * reflProb);
+    B.type = kTypeSpec;
+  } else if (prob_rand(refrProb, u[3])) {
+    B.nOrig = (orig + (dist + kBias) * dir) + refrDir * kBias;
+    B.nDir = refrDir;
+    float cosine = dot(-1.f * nl, refrDir);
+    B.lmt = (cosine * m.diff) / (refrProb * (1.f - reflProb));
+    B.type = kTypeSpec;
+  } else {
+    f3 dd = cos_dir(u[4], u[5], nl);
+    B.nOrig = (orig + dist * dir) + dd * kBias;
+    B.nDir = dd;
+    B.lmt = (kPi * (m.diff * kInvPi)) / ((1.f - refrProb) * (1.f - reflProb));
+    B.type = kTypeDiff;
+  }
+}
+
+// light-vertex cache record: 6 float4
+//   {pos, specular} {norm, metallic} {irrad, roughness} {irradDir, 0} {diff, 0} {emissive, 0}
+struct LV {
+  f3 pos, norm, irrad, irradDir, diff, emis;
+  float spec, metal, rough;
+};
+__device__ __forceinline__ void store_lv(float4* c, const LV& v) {
+  c[0] = st4(v.pos, v.spec);
+  c[1] = st4(v.norm, v.metal);
+  c[2] = st4(v.irrad, v.rough);
+  c[3] = st4(v.irradDir, 0.f);
+  c[4] = st4(v.diff, 0.f);
+  c[5] = st4(v.emis, 0.f);
+}
+__device__ __forceinline__ LV load_lv(const float4* c) {
+  LV v;
+  float4 a = c[0], b = c[1], d = c[2], e = c[3], f = c[4], g = c[5];
+  v.pos = ld3(a);
+  v.spec = a.w;
+  v.norm = ld3(b);
+  v.metal = b.w;
+  v.irrad = ld3(d);
+  v.rough = d.w;
+  v.irradDir = ld3(e);
+  v.diff = ld3(f);
+  v.emis = ld3(g);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Light pass: one CTA, one thread per light subpath.  Cache slots are handed
+// out exactly as the reference's stable remove_if does: a surviving path's
+// position in the stream equals the number of surviving paths with a lower
+// index, i.e. an exclusive scan of the "alive" flags.
+__global__ void __launch_bounds__(1024) k_light(DevScene S, FrameArgs a, float4* cache, uint32_t cacheCap,
+                                                DevCounters* ctr) {
+  using namespace gb;
+  __shared__ uint32_t warpCnt[32];
+  const uint32_t x = threadIdx.x;
+  const uint32_t NL = a.lightPaths;
+  const uint32_t lane = x & 31, warp = x >> 5, nWarps = (blockDim.x + 31) >> 5;
+  bool alive = (x < NL) && (S.lightN > 0);
+  f3 orig = mk(0.f, 0.f, 0.f), dir = orig, outMul = mk(1.f, 1.f, 1.f), sample = orig;
+  uint32_t depth = 0;
+  if (alive) {
+    float u[8];
+    draw8(a.key0, a.key1, x, a.frame, kLightGen, 0, 0, u);
+    uint32_t id = (uint32_t)(u[0] * (float)S.lightN);
+    if (id >= S.lightN) id = S.lightN - 1;
+    float lw = u[1], lu = u[2];
+    if (lw + lu > 1.0f) {
+      lw = 1.f - lw;
+      lu = 1.f - lu;
+    }
+    float lvv = 1.f - lw - lu;
+    Surf sf = load_surf(S, S.lightTri[id], lw, lu, lvv, true);
+    Mat m = load_mat(S, sf.mat);
+    dir = cos_dir(u[3], u[4], sf.norm);
+    orig = sf.pos + kBias * sf.norm;
+    sample = m.emis;
+    LV v;
+    v.pos = sf.pos;
+    v.norm = sf.norm;
+    v.irrad = m.emis;
+    v.irradDir = mk(0.f, 0.f, 0.f);
+    v.diff = m.diff;
+    v.emis = m.emis;
+    v.spec = m.spec;
+    v.metal = m.metal;
+    v.rough = m.rough;
+    store_lv(cache + 6 * (size_t)x, v);
+  }
+  uint32_t size = (S.lightN > 0) ? NL : 0;
+  __syncthreads();
+  for (;;) {
+    uint32_t bal = __ballot_sync(0xffffffffu, alive);
+    if (lane == 0) warpCnt[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (uint32_t w = 0; w < nWarps; w++) {
+      uint32_t c = warpCnt[w];
+      if (w < warp) before += c;
+      total += c;
+    }
+    __syncthreads();
+    if (total == 0) break;
+    if (alive) {
+      uint32_t slot = size + before + __popc(bal & lanemask_lt());
+      if (slot >= cacheCap) {
+        atomicOr(&ctr->errFlags, 1u);
+        alive = false;
+      } else {
+        float4* cs = cache + 6 * (size_t)slot;
+        TraceHit h;
+        uint32_t nn = 0, nt = 0;
+        if (!trace_ref<false, false>(S, orig, dir, kInf, kBias, false, h, nn, nt)) {
+          const float4* home = cache + 6 * (size_t)x;  // :358-362
+          for (int k = 0; k < 6; k++) cs[k] = home[k];
+          alive = false;
+        } else {
+          float u[8];
+          draw8(a.key0, a.key1, x, a.frame, kLightBounce, depth, 0, u);
+          float hw = 1.f - h.u - h.v;
+          Surf sf = load_surf(S, h.tri, hw, h.u, h.v, true);
+          Mat m = load_mat(S, sf.mat);
+          Bounce B;
+          sample_bounce(orig, dir, h.t, sf.norm, m, u, false, B);
+          LV v;
+          v.irrad = (B.type != kTypeDiff) ? mk(0.f, 0.f, 0.f) : sample;
+          v.irradDir = -1.f * dir;
+          v.norm = (dot(B.nDir, B.nl) < 0.f) ? -1.f * B.nl : B.nl;
+          v.pos = sf.pos;
+          v.diff = m.diff;
+          v.emis = m.emis;
+          v.spec = m.spec;
+          v.metal = m.metal;
+          v.rough = m.rough;
+          store_lv(cs, v);
+          sample = m.emis + vmul(sample, B.lmt);
+          float contrib = length(outMul) * length(B.lmt);
+          if (length(m.emis) > 0.f) contrib = 0.f;
+          if (u[6] > contrib || depth + 1 >= a.lightDepth) {
+            alive = false;
+          } else {
+            outMul = vmul(outMul, B.lmt);
+            dir = B.nDir;
+            orig = B.nOrig;
+            depth++;
+          }
+        }
+      }
+    }
+    size += total;
+    __syncthreads();
+  }
+  if (x == 0) ctr->cacheSize = size;
+}
+
+// ---------------------------------------------------------------------------
+// Camera rays, one per pixel (pt_genPathQueue_kernel, :619-640).
+__global__ void k_camera(FrameArgs a, RenderBuffers b) {
+  using namespace gb;
+  const uint32_t np = a.width * a.height;
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p == 0) {
+    b.ctr->wave[0] = np;
+    b.ctr->paths = np;
+  }
+  if (p >= np) return;
+  const uint32_t x = p % a.width, y = p / a.width;
+  float u[4];
+  draw4(a.key0, a.key1, p, a.frame, kCamera, 0, 0, 0, u);
+  const float W = a.W, H = a.H, th = a.tanHalf;
+  float cu = ((((2.f * ((float)x + 0.5f)) / W) - 1.f) * th * W) / H;
+  float cv = (((2.f * ((float)y + 0.5f)) / H) - 1.f) * th;
+  float au = cu + ((u[0] - 0.5f) / H) * th;
+  float av = cv + ((u[1] - 0.5f) / H) * th;
+  f3 R = mk(a.camRight[0], a.camRight[1], a.camRight[2]);
+  f3 U = mk(a.camUp[0], a.camUp[1], a.camUp[2]);
+  f3 D = mk(a.camDir[0], a.camDir[1], a.camDir[2]);
+  f3 dir = normalize((R * au + U * av) + D);
+  Wave w = b.wave[0];
+  w.o[p] = make_float4(a.camPos[0], a.camPos[1], a.camPos[2], __uint_as_float(p));
+  w.d[p] = st4u(dir, p);
+  w.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+  w.smp[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+  b.res[p] = make_float4(0.f, 0.f, 0.f, __uint_as_float(0u));
+  b.slotPix[p] = p;
+  b.slotSmp[p] = 0;
+  if (a.gbuffer) {
+    b.gbuf[3 * (size_t)p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    b.gbuf[3 * (size_t)p + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    b.gbuf[3 * (size_t)p + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+__device__ __forceinline__ void warp_add_u64(unsigned long long* dst, uint32_t v) {
+  uint32_t s = v;
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst, (unsigned long long)s);
+}
+
+// ---------------------------------------------------------------------------
+// Closest-hit traversal of one wave.
+template <bool kCount>
+__global__ void __launch_bounds__(kBlock) k_trace(DevScene S, RenderBuffers b, int in) {
+  const uint32_t n = b.ctr->wave[in];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    b.ctr->wave[in ^ 1] = 0;
+    b.ctr->shadow = 0;
+  }
+  const Wave w = b.wave[in];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    uint32_t nn = 0, nt = 0;
+    if (i < n) {
+      float4 o = w.o[i], d = w.d[i];
+      TraceHit h;
+      float4 r = make_float4(-1.f, 0.f, 0.f, 0.f);
+      if (trace_ref<false, kCount>(S, ld3(o), ld3(d), gb::kInf, gb::kBias, false, h, nn, nt))
+        r = make_float4(h.t, __uint_as_float(h.tri), h.u, h.v);
+      b.hit[i] = r;
+    }
+    if (kCount) {
+      warp_add_u64(&b.ctr->nodes, nn);
+      warp_add_u64(&b.ctr->tris, nt);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Shading of one wave (pt_traceSample_kernel after TracePrimitive) and the
+// connection set-up of GetLightFromRandLightVertices / pt_connectEyeLightPath_kernel.
+__global__ void __launch_bounds__(kBlock) k_shade(DevScene S, FrameArgs a, RenderBuffers b, int in, uint32_t depth) {
+  using namespace gb;
+  const uint32_t n = b.ctr->wave[in];
+  const uint32_t cacheSize = b.ctr->cacheSize;
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.ctr->rays, (unsigned long long)n);
+  const Wave w = b.wave[in];
+  const Wave wo = b.wave[in ^ 1];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t lane = threadIdx.x & 31;
+  const f3 env = mk(a.env[0], a.env[1], a.env[2]);
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    bool cont = false, conn = false;
+    float4 outO, outD, outT, outS, shA, shB, shC;
+    if (i < n) {
+      const float4 o4 = w.o[i], d4 = w.d[i], t4 = w.thr[i], s4 = w.smp[i], h4 = b.hit[i];
+      const uint32_t slot = __float_as_uint(o4.w);
+      const uint32_t pix = __float_as_uint(d4.w);
+      f3 orig = ld3(o4), dir = ld3(d4), outMul = ld3(t4), pathSample = ld3(s4);
+      if (h4.x < 0.f) {  // miss (:537-542), plus the optional environment term
+        if (a.useEnv) pathSample = pathSample + vmul(env, outMul);
+        float4 r = b.res[slot];
+        r = make_float4(r.x + pathSample.x, r.y + pathSample.y, r.z + pathSample.z,
+                        __uint_as_float(__float_as_uint(r.w) + 1u));
+        b.res[slot] = r;
+      } else {
+        const uint32_t smp = b.slotSmp[slot];
+        float u[8];
+        draw8(a.key0, a.key1, pix, a.frame, kEyeBounce, depth, smp, u);
+        const float hu = h4.z, hv = h4.w, hw = 1.f - hu - hv;
+        Surf sf = load_surf(S, __float_as_uint(h4.y), hw, hu, hv, a.gbuffer && depth == 0);
+        Mat m = load_mat(S, sf.mat);
+        Bounce B;
+        sample_bounce(orig, dir, h4.x, sf.norm, m, u, a.specPush != 0, B);
+        pathSample = pathSample + vmul(m.emis, outMul);
+        if (a.gbuffer && depth == 0) {  // AdapBilatAtomic.cu:471-476
+          b.gbuf[3 * (size_t)slot] = st4(sf.pos, 0.f);
+          b.gbuf[3 * (size_t)slot + 1] = st4(B.nl, 0.f);
+          b.gbuf[3 * (size_t)slot + 2] = st4(m.diff, 0.f);
+        }
+        const f3 inMul = outMul;
+        float contrib = length(outMul) * length(B.lmt);
+        if (length(m.emis) > 0.f) contrib = 0.f;
+        if (u[6] > contrib || depth + 1 >= a.eyeDepth) {
+          float4 r = b.res[slot];
+          r = make_float4(r.x + pathSample.x, r.y + pathSample.y, r.z + pathSample.z,
+                          __uint_as_float(__float_as_uint(r.w) + 1u));
+          b.res[slot] = r;
+        } else {
+          cont = true;
+          outMul = vmul(outMul, B.lmt);
+          outO = st4u(B.nOrig, slot);
+          outD = st4u(B.nDir, pix);
+          outT = st4(outMul, 0.f);
+          outS = st4(pathSample, 0.f);
+          if (B.type == kTypeDiff && cacheSize > 0) {
+            // connection (:665-723): everything but the visibility test
+            f3 pos = B.nOrig + B.nl * kBias;
+            uint32_t li = (uint32_t)(u[7] * (float)cacheSize);
+            if (li >= cacheSize) li = cacheSize - 1;
+            LV lv = load_lv(b.cache + 6 * (size_t)li);
+            f3 toDir = normalize(lv.pos - pos);
+            float toDist = length(lv.pos - pos);
+            if (length(lv.irrad) > 0.f && dot(B.nl, toDir) > 0.f) {
+              f3 irrad, irradDir;
+              if (toDist > kFltEps) {
+                irrad = shading(-1.f * toDir, lv.irradDir, lv.irrad, lv.norm, lv.diff, lv.metal, lv.rough, lv.spec,
+                                1.f, 1.f) +
+                        lv.emis;
+                irradDir = toDir;
+              } else {
+                irrad = lv.irrad;
+                irradDir = -1.f * lv.irradDir;
+              }
+              f3 c = vmax0(shading(-1.f * dir, irradDir, irrad, B.nl, m.diff, m.metal, m.rough, m.spec,
+                                   1.f - m.trans, 1.f));
+              if (length(c) > 0.f) {
+                conn = true;
+                shA = st4u(pos, slot);
+                shB = st4(toDir, toDist - kBias);
+                shC = st4(vmul(c, inMul), 0.f);
+              }
+            }
+          }
+        }
+      }
+    }
+    // append survivors / connection requests: one atomic per warp
+    const uint32_t mc = __ballot_sync(0xffffffffu, cont);
+    if (mc) {
+      uint32_t basej = 0;
+      if (lane == 0) basej = atomicAdd(&b.ctr->wave[in ^ 1], __popc(mc));
+      basej = __shfl_sync(0xffffffffu, basej, 0);
+      if (cont) {
+        uint32_t j = basej + __popc(mc & lanemask_lt());
+        wo.o[j] = outO;
+        wo.d[j] = outD;
+        wo.thr[j] = outT;
+        wo.smp[j] = outS;
+      }
+    }
+    const uint32_t ms = __ballot_sync(0xffffffffu, conn);
+    if (ms) {
+      uint32_t basej = 0;
+      if (lane == 0) basej = atomicAdd(&b.ctr->shadow, __popc(ms));
+      basej = __shfl_sync(0xffffffffu, basej, 0);
+      if (conn) {
+        uint32_t j = basej + __popc(ms & lanemask_lt());
+        b.sh[3 * (size_t)j] = shA;
+        b.sh[3 * (size_t)j + 1] = shB;
+        b.sh[3 * (size_t)j + 2] = shC;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Shadow rays: any-hit walk (same visiting order; stops at the first hit
+// closer than maxDist, which is exactly when the closest-hit walk would
+// report a hit); unoccluded connections add to their path (:716-721).
+template <bool kCount>
+__global__ void __launch_bounds__(kBlock) k_shadow(DevScene S, RenderBuffers b) {
+  const uint32_t n = b.ctr->shadow;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(&b.ctr->rays, (unsigned long long)n);
+    atomicAdd(&b.ctr->shadowRays, (unsigned long long)n);
+  }
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t j = base + threadIdx.x;
+    uint32_t nn = 0, nt = 0;
+    if (j < n) {
+      float4 A = b.sh[3 * (size_t)j], B = b.sh[3 * (size_t)j + 1];
+      TraceHit h;
+      if (!trace_ref<true, kCount>(S, ld3(A), ld3(B), B.w, gb::kBias, false, h, nn, nt)) {
+        float4 C = b.sh[3 * (size_t)j + 2];
+        const uint32_t slot = __float_as_uint(A.w);
+        float4 r = b.res[slot];
+        b.res[slot] = make_float4(r.x + C.x, r.y + C.y, r.z + C.z, __uint_as_float(__float_as_uint(r.w) + 4u));
+      }
+    }
+    if (kCount) {
+      warp_add_u64(&b.ctr->nodesS, nn);
+      warp_add_u64(&b.ctr->trisS, nt);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Running mean of one path per pixel (pt_applyPathQueueResult_kernel :741-778);
+// with G-buffer planes, also the count-weighted first-hit means
+// (AdapBilatAtomic.cu:929-966).
+__global__ void k_apply(FrameArgs a, RenderBuffers b, float* result, uint32_t* sampleN, float* gpos, float* gnorm,
+                        float* gdiff) {
+  const uint32_t np = a.width * a.height;
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const float4 r = b.res[p];
+  const uint32_t n = __float_as_uint(r.w);
+  if (n == 0) return;
+  uint32_t old = (a.frame == 0) ? 0u : sampleN[p];
+  if (a.frame == 0) sampleN[p] = 0;
+  const uint32_t nn = old + n;
+  if (!(nn > old)) return;
+  if (isinf(r.x) || isinf(r.y) || isinf(r.z)) return;
+  const float rInf = 1.f / (float)nn;
+  const float oInf = (float)old * rInf;
+  float* q = result + 3 * (size_t)p;
+  q[0] = fmaxf(rInf * r.x + oInf * q[0], 0.f);
+  q[1] = fmaxf(rInf * r.y + oInf * q[1], 0.f);
+  q[2] = fmaxf(rInf * r.z + oInf * q[2], 0.f);
+  sampleN[p] = nn;
+  if (gpos) {
+    float* planes[3] = {gpos, gnorm, gdiff};
+    const float fn = (float)n;
+    for (int k = 0; k < 3; k++) {
+      float4 g = b.gbuf[3 * (size_t)p + k];
+      float* o = planes[k] + 3 * (size_t)p;
+      o[0] = rInf * (g.x * fn) + oInf * o[0];
+      o[1] = rInf * (g.y * fn) + oInf * o[1];
+      o[2] = rInf * (g.z * fn) + oInf * o[2];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stand-alone TracePrimitive for caller-supplied rays.
+template <bool kCount>
+__global__ void k_trace_rays(DevScene S, const float* rays, uint32_t n, float maxDist, float eps, int cullback,
+                             float* t, int32_t* tri, float* w, float* u, float* v, uint32_t* nodes,
+                             uint32_t* trisTested) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* r = rays + 6 * (size_t)i;
+  TraceHit h;
+  uint32_t nn = 0, nt = 0;
+  bool hit = trace_ref<false, kCount>(S, mk(r[0], r[1], r[2]), mk(r[3], r[4], r[5]), maxDist, eps, cullback != 0,
+                                      h, nn, nt);
+  t[i] = hit ? h.t : -1.f;
+  tri[i] = hit ? (int32_t)h.tri : -1;
+  w[i] = hit ? h.w : 0.f;
+  u[i] = hit ? h.u : 0.f;
+  v[i] = hit ? h.v : 0.f;
+  if (kCount) {
+    nodes[i] = nn;
+    trisTested[i] = nt;
+  }
+}
+
+int g_sm = 0;
+
+uint32_t grid_for(const void* kernel) {
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kBlock, 0);
+  if (per < 1) per = 1;
+  return (uint32_t)(sm_count() * per);
+}
+
+}  // namespace
+
+int sm_count() {
+  if (!g_sm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sm <= 0) g_sm = 1;
+  }
+  return g_sm;
+}
+
+cudaError_t launch_light_pass(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, cudaStream_t st) {
+  uint32_t threads = ((a.lightPaths + 31) / 32) * 32;
+  if (threads == 0) threads = 32;
+  k_light<<<1, threads, 0, st>>>(S, a, b.cache, b.cacheCap, b.ctr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream_t st) {
+  const uint32_t np = a.width * a.height;
+  k_camera<<<(np + kBlock - 1) / kBlock, kBlock, 0, st>>>(a, b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trace(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, cudaStream_t st) {
+  if (a.counting) {
+    static uint32_t g = grid_for((const void*)k_trace<true>);
+    k_trace<true><<<g, kBlock, 0, st>>>(S, b, in);
+  } else {
+    static uint32_t g = grid_for((const void*)k_trace<false>);
+    k_trace<false><<<g, kBlock, 0, st>>>(S, b, in);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t depth,
+                         cudaStream_t st) {
+  static uint32_t g = grid_for((const void*)k_shade);
+  k_shade<<<g, kBlock, 0, st>>>(S, a, b, in, depth);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shadow(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, cudaStream_t st) {
+  if (a.counting) {
+    static uint32_t g = grid_for((const void*)k_shadow<true>);
+    k_shadow<true><<<g, kBlock, 0, st>>>(S, b);
+  } else {
+    static uint32_t g = grid_for((const void*)k_shadow<false>);
+    k_shadow<false><<<g, kBlock, 0, st>>>(S, b);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_apply(const FrameArgs& a, const RenderBuffers& b, float* result, uint32_t* sampleN, float* gpos,
+                         float* gnorm, float* gdiff, cudaStream_t st) {
+  const uint32_t np = a.width * a.height;
+  k_apply<<<(np + kBlock - 1) / kBlock, kBlock, 0, st>>>(a, b, result, sampleN, gpos, gnorm, gdiff);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trace_rays(const DevScene& S, const float* rays, uint32_t n, float maxDist, float eps, int cullback,
+                              float* t, int32_t* tri, float* w, float* u, float* v, uint32_t* nodes,
+                              uint32_t* trisTested, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  uint32_t grid = (n + kBlock - 1) / kBlock;
+  if (nodes && trisTested)
+    k_trace_rays<true><<<grid, kBlock, 0, st>>>(S, rays, n, maxDist, eps, cullback, t, tri, w, u, v, nodes,
+                                                  trisTested);
+  else
+    k_trace_rays<false><<<grid, kBlock, 0, st>>>(S, rays, n, maxDist, eps, cullback, t, tri, w, u, v, nodes,
+                                                   trisTested);
+  return cudaGetLastError();
+}
+
+}  // namespace gbpt

@@ -1,0 +1,111 @@
+// Device data layouts and kernel launchers of libgbpt (host-visible part).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace gbpt {
+
+// Scene in HBM.  The BVH node keeps the reference's compact layout
+// (src/cudaRTCommon.cu:527-541: float4 min/max + two uint words) folded into
+// one 32-byte record: {min.xyz, offOrTs}, {max.xyz, triN}.  Intersection data
+// is the reference's p0 / p1-p0 / p2-p0 (:503-513), 48 bytes per triangle.
+// Shading data is gathered per triangle in BVH order (5 float4, 80 bytes):
+//   {n0.xyz, p0.x} {n1.xyz, p0.y} {n2.xyz, p0.z} {p1.xyz, mat} {p2.xyz, 0}
+// so a hit reads one contiguous record instead of RTTriangle + 3 RTVertex.
+// Materials: {diffuse.xyz, transparency} {emissive.xyz, specular}
+//            {metallic, roughness, 0, 0}.
+struct DevScene {
+  const float4* nodes = nullptr;
+  const float4* tris = nullptr;
+  const float4* shade = nullptr;
+  const float4* mats = nullptr;
+  const uint32_t* lightTri = nullptr;
+  uint32_t nodeN = 0, triN = 0, lightN = 0, matN = 0;
+};
+
+// Counters shared by the kernels of one renderer (device memory).
+struct DevCounters {
+  uint32_t wave[2];       // paths in the two ping-pong wave buffers
+  uint32_t shadow;        // connection (shadow) rays queued this bounce
+  uint32_t cacheSize;     // light-vertex cache entries
+  uint32_t paths;         // camera paths of the current frame
+  uint32_t errFlags;      // bit 0: light cache overflow, bit 1: bounds
+  uint32_t pad[2];
+  unsigned long long rays, nodes, tris;  // cumulative work counters (closest-hit walks)
+  unsigned long long shadowRays, nodesS, trisS;  // any-hit (shadow) walks
+  double errSum;          // adaptive: sum of per-pixel errors
+};
+
+// Path state of one wavefront (structure of arrays, float4-packed).
+struct Wave {
+  float4* o;    // origin.xyz, slot (uint bits)
+  float4* d;    // direction.xyz, depth | type << 8
+  float4* thr;  // throughput (pathOutMulTerm).xyz
+  float4* smp;  // carried emission (pathSample).xyz
+};
+
+struct FrameArgs {
+  float camPos[3], camDir[3], camUp[3], camRight[3];
+  float tanHalf, W, H;
+  uint32_t width, height, frame;
+  uint32_t key0, key1;
+  uint32_t eyeDepth, lightDepth, lightPaths;
+  float env[3];
+  uint32_t specPush;    // adaptive variant: spec reflection origin pushed along reflDir
+  uint32_t gbuffer;     // record first-hit position/normal/diffuse
+  uint32_t counting;    // node/triangle counters
+  uint32_t useEnv;      // env != 0: add env * throughput on a miss
+};
+
+struct RenderBuffers {
+  Wave wave[2];
+  float4* hit;          // t, tri bits, u, v (t < 0: miss)
+  float4* sh;           // 3 per entry: {origin, slot} {dir, maxDist} {weighted contribution}
+  float4* res;          // per slot: acc.xyz, n bits
+  float4* gbuf;         // per slot: 3 float4 (pos, normal, diffuse) when gbuffer
+  uint32_t* slotPix;    // per slot pixel id
+  uint32_t* slotSmp;    // per slot sample id
+  float4* cache;        // light vertices, 6 float4 each
+  DevCounters* ctr;
+  uint32_t cap;         // slots
+  uint32_t cacheCap;    // light vertices
+};
+
+// wavefront kernels (kernels_wave.cu)
+cudaError_t launch_light_pass(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, cudaStream_t st);
+cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream_t st);
+cudaError_t launch_trace(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, cudaStream_t st);
+cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t depth,
+                         cudaStream_t st);
+cudaError_t launch_shadow(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, cudaStream_t st);
+cudaError_t launch_apply(const FrameArgs& a, const RenderBuffers& b, float* result, uint32_t* sampleN, float* gpos,
+                         float* gnorm, float* gdiff, cudaStream_t st);
+cudaError_t launch_trace_rays(const DevScene& S, const float* rays, uint32_t n, float maxDist, float eps, int cullback,
+                              float* t, int32_t* tri, float* w, float* u, float* v, uint32_t* nodes,
+                              uint32_t* trisTested, cudaStream_t st);
+
+// adaptive sampling and filter kernels (kernels_adapt.cu)
+struct AdaptBuffers {
+  float* err;          // W*H
+  uint32_t* cnt;       // W*H sample counts
+  uint32_t* off;       // W*H exclusive offsets
+  uint32_t* blockSum;  // per scan block
+  double* partial;     // per reduce block
+  float* filtered;     // W*H*3
+};
+cudaError_t launch_bilateral(const float* color, const float* pos, const float* norm, const float* emit, uint32_t W,
+                             uint32_t H, float ceud, float peud, float neud, float eeud, uint32_t radius,
+                             const float* g, float* out, cudaStream_t st);
+cudaError_t launch_adapt_budget(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab,
+                                const float* result, const uint32_t* sampleN, uint32_t desired, cudaStream_t st);
+cudaError_t launch_adapt_accum(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab, float* result,
+                               uint32_t* sampleN, float* gpos, float* gnorm, float* gdiff, cudaStream_t st);
+uint32_t adapt_scan_blocks(uint32_t np);
+uint32_t adapt_reduce_blocks(uint32_t np);
+cudaError_t launch_fmath(int which, const float* x, uint32_t n, float* out, cudaStream_t st);
+cudaError_t launch_philox(const uint32_t* ctr, uint32_t n, uint32_t k0, uint32_t k1, uint32_t* out, cudaStream_t st);
+
+int sm_count();
+
+}  // namespace gbpt

@@ -1,0 +1,215 @@
+/*
+ * gbpt -- GB300-native streaming bidirectional path tracer, C ABI.
+ *
+ * Drop-in boundary for the BDPT hot path of CudaPT.  Every entry point below
+ * names the reference interface it replaces (paths are relative to the
+ * CudaPT repository).  Plain pointers and sizes only; no C++ or framework
+ * types cross this boundary.  All functions return a gbpt_status; the text of
+ * the last error of the calling thread is available from
+ * gbpt_last_error_string().
+ *
+ * Threading: a scene or renderer handle is used by one host thread at a time;
+ * different handles may be driven from different threads.  Each renderer owns
+ * a CUDA stream; gbpt_render() returns when the frame is complete and, if an
+ * output pointer is given, copied.
+ */
+#ifndef GBPT_H
+#define GBPT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gbpt_status {
+  GBPT_OK = 0,
+  GBPT_ERR_INVALID_ARG = 1, /* bad handle, size or pointer */
+  GBPT_ERR_OOM = 2,         /* device or host allocation failed / admission refused */
+  GBPT_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  GBPT_ERR_TIMEOUT = 4,     /* a bounded device wait ran out */
+  GBPT_ERR_BOUNDS = 5,      /* a device-side bounds check tripped */
+  GBPT_ERR_STATE = 6,       /* call not valid in the current state (e.g. no BVH) */
+  GBPT_ERR_NO_DEVICE = 7    /* no CUDA device or the kernels were not built for it */
+} gbpt_status;
+
+/* Scene records, byte-compatible with the reference (include/raytracer.h:58-101). */
+typedef struct gbpt_vertex { /* RTVertex, 44 bytes */
+  float pos[3], norm[3], tan[3], tex[2];
+} gbpt_vertex;
+
+typedef struct gbpt_triangle { /* RTTriangle, 16 bytes */
+  uint32_t v0, v1, v2, mat;
+} gbpt_triangle;
+
+typedef struct gbpt_material { /* RTMaterial (no FULLSPECTRAL), 80 bytes */
+  float diffuse[3], emissive[3];
+  int32_t diffuseTexId, normalTexId, emissiveTexId, matType;
+  float transparency, subsurface, specular, metallic, roughness;
+  float anisotropic, sheen, sheenTint, clearcoat, clearcoatGloss;
+} gbpt_material;
+
+/* Camera of RTRenderer::Render(camPos, camDir, camUp, fov, scene)
+ * (include/raytracer.h:310); fov in radians. */
+typedef struct gbpt_camera {
+  float pos[3], dir[3], up[3];
+  float fov;
+} gbpt_camera;
+
+/* Renderer knobs.  The reference kept these as compile-time defines and GUI
+ * attributes: NORMALRAY_BOUND_MAX / LIGHTRAY_BOUND_MAX
+ * (src/cudaRTBDPTStream.cu:7,10), the 128-path light pass every 3rd frame
+ * (:875-877), and the adaptive attributes of
+ * src/cudaRTBDPTStreamAdapBilatAtomic.cu:26-37.  gbpt_params_default() gives
+ * the reference values. */
+typedef struct gbpt_params {
+  uint32_t seed;            /* Philox4x32-10 key word 0 (default 1234) */
+  uint32_t eye_depth_max;   /* camera-path bounce cap (5) */
+  uint32_t light_depth_max; /* light-path bounce cap (5) */
+  uint32_t light_paths;     /* light subpaths per light pass (128, <= 1024) */
+  uint32_t light_every;     /* light pass when frame % light_every == 0 (3) */
+  float env[3];             /* constant environment radiance on a miss (0) */
+  uint32_t warmup_frames;   /* uniform frames before adaptive sampling (5) */
+  uint32_t desired_n;       /* "Desired Max Sampling" (5) */
+  float filter_color_eud;   /* "Filter Color EuD" (50) */
+  float filter_pos_eud;     /* "Filter Pos EuD" (1) */
+  float filter_norm_eud;    /* "Filter Norm EuD" (0.25) */
+  float filter_diff_eud;    /* "Filter Diff EuD" (0.1) */
+  uint32_t filter_radius;   /* "Filter Radius" (5, <= 31) */
+  uint32_t filter_diffuse;  /* "Filter Diffuse Flag" (0) */
+  float filter_sigma_spatial; /* spatial Gaussian sigma in pixels; <= 0 keeps the
+                                 reference's table built from the colour delta */
+  uint32_t request_id;      /* Philox key word 1 (0) */
+} gbpt_params;
+
+/* Renderer modes: the BDPT entries of the X-macro registry
+ * (include/raytracer.h:13-23). */
+typedef enum gbpt_mode {
+  GBPT_MODE_BDPT_SC = 0,            /* "BDPTSC"                 cudaRTBDPTStream */
+  GBPT_MODE_BDPT_SC_ADAP_BILAT = 1  /* "BDPTSC Adap Bilat PLL"  cudaRTBDPTStreamAdapBilatAtomic */
+} gbpt_mode;
+
+/* Per-frame statistics (the reference's PERFBREAKDOWN timers,
+ * src/cudaRTBDPTStreamAdapBilatAtomic.cu:1409-1536, plus work counters). */
+typedef struct gbpt_stats {
+  uint32_t frame;          /* progressive frame index after this call */
+  uint32_t light_vertices; /* light-vertex cache size used by this frame */
+  uint64_t paths;          /* camera paths traced this frame */
+  uint64_t rays;           /* extension + shadow rays this frame */
+  uint64_t shadow_rays;    /* of which shadow (connection) rays */
+  uint64_t nodes;          /* closest-hit BVH node visits (only with gbpt_set_counting(r, 1)) */
+  uint64_t tris;           /* closest-hit triangle tests (only with counting on) */
+  uint64_t shadow_nodes;   /* any-hit node visits (counting on) */
+  uint64_t shadow_tris;    /* any-hit triangle tests (counting on) */
+  float ms_total;          /* device time of the frame */
+  float ms_light;          /* light pass */
+  float ms_trace;          /* closest-hit traversal kernels */
+  float ms_shade;          /* shading / compaction kernels */
+  float ms_shadow;         /* shadow-ray kernels */
+  float ms_filter;         /* bilateral filter */
+  float ms_adapt;          /* error, budget and accumulation kernels */
+} gbpt_stats;
+
+typedef struct gbpt_scene gbpt_scene;
+typedef struct gbpt_renderer gbpt_renderer;
+
+/* ---- library ------------------------------------------------------------ */
+const char* gbpt_last_error_string(void);
+/* 1 when a usable sm_103 device is present and the kernels load on it. */
+gbpt_status gbpt_device_check(int32_t* ok);
+gbpt_status gbpt_params_default(gbpt_params* p);
+
+/* ---- scene: RTScene (include/raytracer.h:228-290) ------------------------- */
+/* Copies the arrays (RTScene::m_pVertices / m_pTriangles / m_pMaterials).
+ * Replaces RTScene::AddModel's Assimp import (src/raytracer.cpp:238-263):
+ * the caller passes the imported geometry directly. */
+gbpt_status gbpt_scene_create(const gbpt_vertex* verts, uint32_t nv, const gbpt_triangle* tris, uint32_t nt,
+                              const gbpt_material* mats, uint32_t nm, gbpt_scene** out);
+gbpt_status gbpt_scene_destroy(gbpt_scene* s);
+/* NPBVHHelper::CreateBVH + CompactBVH::InitialCompactBVH
+ * (src/bvhhelper.cpp:239-313) and AddModel's triangle reorder
+ * (src/raytracer.cpp:264-281); then the device upload of initAllSceneCudaMem
+ * (src/cudaRTCommon.cu:472-578).  max_depth 32 is the reference default.
+ * build_seconds (optional) receives the host build time. */
+gbpt_status gbpt_scene_build_bvh(gbpt_scene* s, uint32_t max_depth, uint32_t threads, double* build_seconds);
+/* updateAllSceneMaterialsCudaMem (src/cudaRTCommon.cu:580-599) and the
+ * light-triangle rescan updateLightTriCudaMem (src/cudaRTBDPTStream.cu:57-77). */
+gbpt_status gbpt_scene_update_materials(gbpt_scene* s, const gbpt_material* mats, uint32_t nm);
+/* CompactBVH export (include/bvhhelper.h:45-54): node count first (pass NULL
+ * arrays), then bounds[6*nodeN] (min xyz, max xyz), offOrTSTN[2*nodeN],
+ * tri_order[nt] (CreateBVH's return value). */
+gbpt_status gbpt_scene_bvh_info(const gbpt_scene* s, uint32_t* node_count, uint32_t* tri_count,
+                                uint32_t* light_count);
+gbpt_status gbpt_scene_bvh_export(const gbpt_scene* s, float* bounds, uint32_t* off_or_tstn, uint32_t* tri_order);
+
+/* ---- traversal: TracePrimitive (src/cudaRTCommon.cu:66-127) ---------------
+ * Closest hit for n rays given as 6 floats (origin, direction).  rays and the
+ * outputs may be host or device pointers (is_device = 0/1).  t = -1 and
+ * tri = -1 on a miss.  nodes/tris_tested are optional per-ray work counters. */
+gbpt_status gbpt_trace_rays(gbpt_scene* s, const float* rays, uint32_t n, float max_dist, float eps, int32_t cullback,
+                            float* t, int32_t* tri, float* w, float* u, float* v, uint32_t* nodes,
+                            uint32_t* tris_tested, int32_t is_device);
+
+/* ---- renderer: RTRenderer (include/raytracer.h:292-323) -------------------- */
+/* RTRenderer::Init(width, height) + SetRendererMode(mode). */
+gbpt_status gbpt_renderer_create(uint32_t width, uint32_t height, int32_t mode, const gbpt_params* params,
+                                 gbpt_renderer** out);
+gbpt_status gbpt_renderer_destroy(gbpt_renderer* r);
+gbpt_status gbpt_set_mode(gbpt_renderer* r, int32_t mode);
+gbpt_status gbpt_set_params(gbpt_renderer* r, const gbpt_params* params);
+gbpt_status gbpt_get_params(const gbpt_renderer* r, gbpt_params* params);
+/* RTRenderer::Render -> <codename>::Render(camPos, camDir, camUp, fov, scene,
+ * width, height, result) (src/raytracer.cpp:19-31, 610-625;
+ * src/cudaRTBDPTStream.cu:816-951).  Adds one progressive pass; the frame
+ * counter restarts when the camera changes.  out_rgb (may be NULL) receives
+ * width*height*3 floats, row 0 at the bottom; out_is_device selects a device
+ * or host destination.  stats may be NULL. */
+gbpt_status gbpt_render(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, float* out_rgb,
+                        int32_t out_is_device, gbpt_stats* stats);
+/* Adds `frames` passes without copying (benchmarks / progressive runs). */
+gbpt_status gbpt_render_frames(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, uint32_t frames,
+                               gbpt_stats* stats);
+/* RTRenderer::GetResult (include/raytracer.h:311): library-owned host copy of
+ * the last result (refreshed by gbpt_render / gbpt_read_result). */
+const float* gbpt_result(gbpt_renderer* r);
+/* Copies a renderer buffer: 0 result RGB, 1 first-hit position, 2 normal,
+ * 3 diffuse (G-buffer of the adaptive mode), 4 filtered RGB, 5 per-pixel error
+ * (W*H floats), 6 per-pixel sample count (W*H uint32). */
+gbpt_status gbpt_read_buffer(gbpt_renderer* r, int32_t which, void* dst, size_t bytes, int32_t dst_is_device);
+/* Restart progressive accumulation (next frame is frame 0). */
+gbpt_status gbpt_reset(gbpt_renderer* r);
+/* CleanMem (src/cudaRTBDPTStream.cu:780-789): release device buffers now;
+ * they are re-created on the next render. */
+gbpt_status gbpt_clean(gbpt_renderer* r);
+/* Enable per-frame node/triangle counters (costs one atomic per warp and step). */
+gbpt_status gbpt_set_counting(gbpt_renderer* r, int32_t on);
+
+/* ---- attributes: GetAttribute / GetAttribsN (src/raytracer.cpp:19-31) ----- */
+gbpt_status gbpt_attr_count(const gbpt_renderer* r, uint32_t* n);
+gbpt_status gbpt_attr_name(const gbpt_renderer* r, uint32_t index, char* name, size_t cap);
+gbpt_status gbpt_attr_get(const gbpt_renderer* r, const char* name, float* value);
+gbpt_status gbpt_attr_set(gbpt_renderer* r, const char* name, float value);
+
+/* ---- bilateral filter: cudaBilateralFilter (src/cudaBilateralFilter.cu) ----
+ * updateGaussian (:5-24) into g[2*radius+1]. */
+gbpt_status gbpt_gaussian_table(float delta, uint32_t radius, float* g);
+/* bilaterial_posnorm_kernel (:66-101) when emit == NULL, else
+ * bilaterial_posnormemit_kernel (:103-142).  All planes are W*H*3 floats, on
+ * the device when is_device = 1, else on the host; g is a host table of
+ * 2*radius+1 floats. */
+gbpt_status gbpt_bilateral(const float* color, const float* pos, const float* norm, const float* emit,
+                           uint32_t width, uint32_t height, float color_eud, float pos_eud, float norm_eud,
+                           float emit_eud, uint32_t radius, const float* g, float* out, int32_t is_device);
+
+/* ---- device math, exposed for verification -------------------------------
+ * Evaluated by a kernel on host arrays x/out (copied in and out).
+ * which: 0 sin, 1 cos, 2 exp, 3 round-down sqrt, 4 x^5. */
+gbpt_status gbpt_fmath(int32_t which, const float* x, uint32_t n, float* out);
+/* Philox4x32-10 by a kernel: n counters (4 words each) -> 4 words each, host arrays. */
+gbpt_status gbpt_philox(const uint32_t* ctr, uint32_t n, uint32_t k0, uint32_t k1, uint32_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBPT_H */

@@ -1,0 +1,218 @@
+"""CPU oracle of the GB300 BDPT library -- TEST INFRASTRUCTURE ONLY.
+
+A C++ restatement of CudaPT's BDPT hot path (BVH build, traversal, the
+streaming BDPT estimator, the adaptive allocator and the bilateral filter),
+compiled from the sources in this folder by ``build()`` and loaded with
+ctypes.  Only tests/, ``__graft_entry__.smoke()`` and the CPU baseline of
+bench.py use it, always as the checker; the shipped library never loads it.
+
+Parity status: the reference cannot be compiled here (MSVC-only headers,
+legacy texture references), and its repository carries no tests, golden
+vectors or saved images for this path.  The oracle is pinned by the
+published Philox4x32-10 known-answer vectors, by hand-derived golden cases
+(tests/golden/) and by the BVH/traversal invariants the reference code
+implies; the estimator itself is "parity unpinned" against the reference
+binary.
+"""
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force=False):
+    """Compile liboracle.so with the Makefile in this folder."""
+    args = ["make", "-s", "-C", _HERE]
+    if force:
+        args.insert(1, "-B")
+    subprocess.run(args, check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(_LIB_PATH):
+                build()
+            L = ctypes.CDLL(_LIB_PATH)
+            vp, u32, i32, f32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int32, ctypes.c_float
+            L.orc_scene_create.restype = vp
+            L.orc_scene_create.argtypes = [vp, u32, vp, u32, vp, u32, vp]
+            L.orc_scene_destroy.argtypes = [vp]
+            for n in ("orc_scene_node_count", "orc_scene_empty_children", "orc_scene_light_count"):
+                getattr(L, n).restype = u32
+                getattr(L, n).argtypes = [vp]
+            L.orc_scene_export.argtypes = [vp, vp, vp, vp, vp]
+            L.orc_update_materials.argtypes = [vp, vp, u32]
+            L.orc_trace.argtypes = [vp, vp, u32, f32, f32, i32, vp, vp, vp, vp, vp, vp, vp]
+            L.orc_default_params.argtypes = [vp]
+            L.orc_renderer_create.restype = vp
+            L.orc_renderer_create.argtypes = [u32, u32, i32, vp, u32]
+            L.orc_renderer_destroy.argtypes = [vp]
+            L.orc_renderer_set_params.argtypes = [vp, vp]
+            L.orc_render.argtypes = [vp, vp, vp, u32]
+            L.orc_renderer_get.argtypes = [vp, i32, vp]
+            L.orc_renderer_counts.argtypes = [vp, vp, vp]
+            L.orc_renderer_frame.restype = u32
+            L.orc_renderer_frame.argtypes = [vp]
+            L.orc_renderer_stats.argtypes = [vp, vp]
+            L.orc_renderer_light_cache.restype = u32
+            L.orc_renderer_light_cache.argtypes = [vp, vp]
+            L.orc_render_fp64.argtypes = [vp, vp, u32, u32, vp, u32, u32, vp]
+            L.orc_gaussian.argtypes = [f32, u32, vp]
+            L.orc_bilateral.argtypes = [vp, vp, vp, vp, u32, u32, f32, f32, f32, f32, u32, vp, vp]
+            L.orc_philox.argtypes = [vp, u32, u32, vp]
+            L.orc_fmath.argtypes = [i32, vp, u32, vp]
+            _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data if a is not None else None
+
+
+def cam_array(cam):
+    return np.array(list(cam["pos"]) + list(cam["dir"]) + list(cam["up"]) + [cam["fov"]], np.float32)
+
+
+class Scene:
+    """Oracle scene: BVH built by the restated builder, triangles reordered."""
+
+    def __init__(self, verts, tris, mats):
+        self.verts, self.tris, self.mats = verts, tris, mats
+        t = ctypes.c_double(0.0)
+        self.h = lib().orc_scene_create(_p(verts), len(verts), _p(tris), len(tris), _p(mats), len(mats),
+                                        ctypes.addressof(t))
+        if not self.h:
+            raise RuntimeError("oracle BVH build failed")
+        self.build_seconds = t.value
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_scene_destroy(self.h)
+            self.h = None
+
+    @property
+    def node_count(self):
+        return lib().orc_scene_node_count(self.h)
+
+    @property
+    def empty_children(self):
+        return lib().orc_scene_empty_children(self.h)
+
+    @property
+    def light_count(self):
+        return lib().orc_scene_light_count(self.h)
+
+    def export(self):
+        n = self.node_count
+        b = np.zeros((n, 6), np.float32)
+        o = np.zeros((n, 2), np.uint32)
+        order = np.zeros(len(self.tris), np.uint32)
+        isect = np.zeros((len(self.tris), 9), np.float32)
+        lib().orc_scene_export(self.h, _p(b), _p(o), _p(order), _p(isect))
+        return b, o, order, isect
+
+    def update_materials(self, mats):
+        self.mats = mats
+        lib().orc_update_materials(self.h, _p(mats), len(mats))
+
+    def trace(self, rays, max_dist=1e20, eps=1e-9, cullback=False):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        n = len(rays)
+        t = np.zeros(n, np.float32)
+        tid = np.zeros(n, np.int32)
+        w, u, v = (np.zeros(n, np.float32) for _ in range(3))
+        nodes = np.zeros(n, np.uint32)
+        trs = np.zeros(n, np.uint32)
+        lib().orc_trace(self.h, _p(rays), n, max_dist, eps, int(cullback), _p(t), _p(tid), _p(w), _p(u), _p(v),
+                        _p(nodes), _p(trs))
+        return dict(t=t, tri=tid, w=w, u=u, v=v, nodes=nodes, tris=trs)
+
+
+class Renderer:
+    """Oracle renderer: one call of render() adds `frames` progressive passes."""
+
+    def __init__(self, width, height, mode, params, threads=None):
+        self.W, self.H = width, height
+        self.params = np.array(params)
+        self.h = lib().orc_renderer_create(width, height, mode, _p(self.params), threads or os.cpu_count())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_renderer_destroy(self.h)
+            self.h = None
+
+    def render(self, scene, cam, frames=1):
+        c = cam_array(cam)
+        lib().orc_render(self.h, scene.h, _p(c), frames)
+
+    def get(self, which=0):
+        n = self.W * self.H * (1 if which == 5 else 3)
+        out = np.zeros(n, np.float32)
+        lib().orc_renderer_get(self.h, which, _p(out))
+        return out
+
+    def sample_counts(self):
+        sn = np.zeros(self.W * self.H, np.uint32)
+        cn = np.zeros(self.W * self.H, np.uint32)
+        lib().orc_renderer_counts(self.h, _p(sn), _p(cn))
+        return sn, cn
+
+    @property
+    def frame(self):
+        return lib().orc_renderer_frame(self.h)
+
+    def stats(self):
+        s = np.zeros(4, np.uint64)
+        lib().orc_renderer_stats(self.h, _p(s))
+        return dict(paths=int(s[0]), rays=int(s[1]), nodes=int(s[2]), tris=int(s[3]))
+
+    def light_cache(self):
+        n = lib().orc_renderer_light_cache(self.h, None)
+        out = np.zeros((max(n, 1), 21), np.float32)
+        lib().orc_renderer_light_cache(self.h, _p(out))
+        return out[:n]
+
+
+def render_fp64(scene, params, width, height, cam, frames, threads=None):
+    out = np.zeros(width * height * 3, np.float64)
+    c = cam_array(cam)
+    p = np.array(params)
+    lib().orc_render_fp64(scene.h, _p(p), width, height, _p(c), frames, threads or os.cpu_count(), _p(out))
+    return out
+
+
+def gaussian(delta, radius):
+    g = np.zeros(64, np.float32)
+    lib().orc_gaussian(delta, radius, _p(g))
+    return g
+
+
+def bilateral(color, pos, norm, emit, W, H, ceud, peud, neud, eeud, radius, g):
+    out = np.zeros(W * H * 3, np.float32)
+    args = [np.ascontiguousarray(a, np.float32) if a is not None else None for a in (color, pos, norm, emit)]
+    lib().orc_bilateral(*[_p(a) for a in args], W, H, ceud, peud, neud, eeud, radius, _p(g), _p(out))
+    return out
+
+
+def philox(ctr, k0, k1):
+    c = np.array(ctr, np.uint32)
+    out = np.zeros(4, np.uint32)
+    lib().orc_philox(_p(c), k0, k1, _p(out))
+    return out
+
+
+def fmath(which, x):
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros_like(x)
+    lib().orc_fmath({"sin": 0, "cos": 1, "exp": 2, "sqrt_rd": 3, "pow5": 4}[which], _p(x), len(x), _p(out))
+    return out

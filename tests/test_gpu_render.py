@@ -1,0 +1,153 @@
+"""GPU parity of whole frames: plain streaming BDPT and the adaptive +
+bilateral variant against the oracle's per-path restatement."""
+import numpy as np
+import pytest
+
+from helpers import block_means, scene_arrays
+
+pytestmark = pytest.mark.gpu
+
+
+def _render_both(gb, orc, name, W, H, frames, mode=0, **pk):
+    (v, t, m), cam = scene_arrays(name)
+    params = gb.default_params(**pk)
+    s = gb.RTScene(v, t, m).build_bvh()
+    r = gb.RTRenderer(W, H, mode, params)
+    stats = []
+    for _ in range(frames):
+        img = r.render(s, cam).copy()
+        stats.append(r.last_stats)
+    osc = orc.Scene(v, t, m)
+    ref = orc.Renderer(W, H, mode, params)
+    ref.render(osc, cam, frames)
+    return r, ref, img, ref.get(0), stats
+
+
+def test_cornell_light_cache_bitexact(gbdev, orc):
+    (v, t, m), cam = scene_arrays("cornell")
+    params = gbdev.default_params(eye_depth_max=8, light_depth_max=8)
+    s = gbdev.RTScene(v, t, m).build_bvh()
+    r = gbdev.RTRenderer(32, 32, 0, params)
+    r.render(s, cam)
+    n = r.last_stats["light_vertices"]
+    ref = orc.Renderer(32, 32, 0, params)
+    ref.render(orc.Scene(v, t, m), cam, 1)
+    want = ref.light_cache()
+    assert n == len(want) and n > 128
+    got = r.light_cache(n)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_cornell_plain_bitexact(gbdev, orc):
+    r, ref, img, want, stats = _render_both(gbdev, orc, "cornell", 64, 64, 7, eye_depth_max=8, light_depth_max=8)
+    same = np.mean(img.view(np.uint32) == want.view(np.uint32))
+    assert same >= 0.999, same
+    np.testing.assert_allclose(img, want, rtol=1e-4, atol=1e-5)
+    sn_gpu = r.read_buffer(6)
+    sn_ref, _ = ref.sample_counts()
+    assert np.mean(sn_gpu == sn_ref) >= 0.999
+    assert stats[-1]["frame"] == 6 and stats[-1]["paths"] == 64 * 64
+
+
+def test_cornell_statistics_independent_seeds(gbdev, orc):
+    """Different Philox keys: 8x8-block means agree within 3 sigma."""
+    (v, t, m), cam = scene_arrays("cornell")
+    W = H = 64
+    frames = 24
+    pa = gbdev.default_params(eye_depth_max=8, light_depth_max=8, seed=1234)
+    pb = gbdev.default_params(eye_depth_max=8, light_depth_max=8, seed=98765)
+    s = gbdev.RTScene(v, t, m).build_bvh()
+    runs = []
+    for p, dev in ((pa, True), (pb, False), (gbdev.default_params(eye_depth_max=8, light_depth_max=8, seed=555), True)):
+        per = []
+        if dev:
+            r = gbdev.RTRenderer(W, H, 0, p)
+            prevS, prevN = np.zeros(W * H * 3), np.zeros(W * H)
+            for f in range(frames):
+                img = r.render(s, cam).astype(np.float64)
+                N = r.read_buffer(6).astype(np.float64)
+                S = img * np.repeat(N, 3)
+                per.append(block_means(S - prevS, W, H) / np.maximum(
+                    block_means(np.repeat(N - prevN, 3), W, H), 1e-9))
+                prevS, prevN = S, N
+        else:
+            ref = orc.Renderer(W, H, 0, p)
+            osc = orc.Scene(v, t, m)
+            prevS, prevN = np.zeros(W * H * 3), np.zeros(W * H)
+            for f in range(frames):
+                ref.render(osc, cam, 1)
+                img = ref.get(0).astype(np.float64)
+                N = ref.sample_counts()[0].astype(np.float64)
+                S = img * np.repeat(N, 3)
+                per.append(block_means(S - prevS, W, H) / np.maximum(
+                    block_means(np.repeat(N - prevN, 3), W, H), 1e-9))
+                prevS, prevN = S, N
+        per = np.array(per)
+        runs.append((per.mean(0), per.std(0, ddof=1) / np.sqrt(frames)))
+    (m1, s1), (m2, s2), (m3, s3) = runs
+    z12 = np.abs(m1 - m2) / np.sqrt(s1 ** 2 + s2 ** 2 + 1e-12)
+    z13 = np.abs(m1 - m3) / np.sqrt(s1 ** 2 + s3 ** 2 + 1e-12)
+    assert np.mean(z12 < 3) >= 0.97, np.mean(z12 < 3)
+    assert np.mean(z13 < 3) >= 0.97, np.mean(z13 < 3)
+
+
+def test_interior_plain_matches(gbdev, orc):
+    r, ref, img, want, stats = _render_both(gbdev, orc, "interior", 96, 72, 4, eye_depth_max=10, light_depth_max=10)
+    same = np.mean(img.view(np.uint32) == want.view(np.uint32))
+    assert same >= 0.995, same
+    assert np.abs(img.mean() - want.mean()) <= 1e-3 * max(want.mean(), 1e-6)
+
+
+def test_env_term(gbdev, orc):
+    """Constant environment on a miss (scene open at z=1: Cornell)."""
+    r, ref, img, want, _ = _render_both(gbdev, orc, "cornell", 48, 48, 3, eye_depth_max=8, light_depth_max=8,
+                                        env=(0.1, 0.1, 0.1))
+    assert np.mean(img.view(np.uint32) == want.view(np.uint32)) >= 0.999
+
+
+def test_adaptive_matches(gbdev, orc):
+    r, ref, img, want, stats = _render_both(gbdev, orc, "cornell", 64, 48, 5, mode=1, eye_depth_max=8,
+                                            light_depth_max=8, warmup_frames=2, filter_radius=4)
+    cnt_ref = ref.sample_counts()[1]
+    assert cnt_ref.sum() > 0
+    np.testing.assert_allclose(r.read_buffer(1), ref.get(1), rtol=1e-5, atol=1e-6)   # G-buffer position
+    np.testing.assert_allclose(r.read_buffer(4), ref.get(4), rtol=1e-4, atol=1e-5)   # filtered
+    same = np.mean(img.view(np.uint32) == want.view(np.uint32))
+    assert same >= 0.99, same
+    assert abs(img.mean() - want.mean()) <= 2e-3 * want.mean()
+
+
+def test_bilateral_kernel_bitexact(gbdev, orc):
+    rng = np.random.Generator(np.random.PCG64(21))
+    W, H = 77, 45
+    planes = [rng.random(W * H * 3).astype(np.float32) for _ in range(4)]
+    L = gbdev._native.load()
+    for radius, emit, delta in ((4, False, 3.0), (5, True, 50.0), (2, False, 1.0)):
+        g = np.zeros(64, np.float32)
+        gbdev._native.check(L.gbpt_gaussian_table(delta, radius, g.ctypes.data))
+        gref = orc.gaussian(delta, radius)
+        assert np.array_equal(g[: 2 * radius + 1], gref[: 2 * radius + 1])
+        out = np.zeros(W * H * 3, np.float32)
+        e = planes[3] if emit else None
+        gbdev._native.check(L.gbpt_bilateral(planes[0].ctypes.data, planes[1].ctypes.data, planes[2].ctypes.data,
+                                             e.ctypes.data if emit else None, W, H, 0.5, 1.0, 0.25, 0.1, radius,
+                                             g.ctypes.data, out.ctypes.data, 0))
+        want = orc.bilateral(planes[0], planes[1], planes[2], e, W, H, 0.5, 1.0, 0.25, 0.1, radius, gref)
+        assert np.array_equal(out.view(np.uint32), want.view(np.uint32)), (radius, emit)
+
+
+def test_errors_are_reported(gbdev):
+    import cudapt_gb300 as gb
+    (v, t, m), cam = scene_arrays("cornell")
+    bad = t.copy()
+    bad["v0"][0] = 10 ** 6
+    with pytest.raises(gb.GbptError):
+        gb.RTScene(v, bad, m)
+    s = gb.RTScene(v, t, m)
+    r = gb.RTRenderer(16, 16)
+    with pytest.raises(gb.GbptError, match="BVH"):
+        r.render(s, cam)
+    with pytest.raises(gb.GbptError):
+        gb.RTRenderer(16, 16, params=gb.default_params(light_paths=5000))
+    with pytest.raises(gb.GbptError):
+        r.attr_set("No Such Attribute", 1.0)

@@ -1,0 +1,63 @@
+"""Regenerate the golden fixtures of tests/golden/ (run in the build container).
+
+Inputs:
+  * the reference's own Cornell asset ``asset/model/cornell_box_with_sphere.obj``
+    (416 faces -> 792 triangles), read from the CudaPT checkout given on the
+    command line (default /root/reference), positions only;
+  * the 36-triangle procedural Cornell box of cudapt_gb300.scenes.
+
+Outputs (all produced by the CPU oracle, FP32 float contract):
+  obj_cornell.npz   mesh, BVH (bounds/offsets/order) and 1024 traced rays
+  cornell_frames.npz 3 progressive frames of a 24x24 plain-BDPT render and
+                     the light-vertex cache of frame 0
+The Philox4x32-10 known-answer vectors are the published Random123 ones and
+live in the test itself.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from cudapt_gb300 import layouts, objio, scenes  # noqa: E402
+
+
+def main(ref_root):
+    obj = os.path.join(ref_root, "asset", "model", "cornell_box_with_sphere.obj")
+    v, t, m = objio.load_obj(obj, with_materials=False)
+    sc = oracle.Scene(v, t, m)
+    b, o, order, isect = sc.export()
+    rng = np.random.Generator(np.random.PCG64(2024))
+    p = v["pos"]
+    lo, hi = p.min(0), p.max(0)
+    orig = (lo + (hi - lo) * rng.random((1024, 3))).astype(np.float32)
+    d = rng.normal(size=(1024, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([orig, d.astype(np.float32)], 1).astype(np.float32)
+    hits = sc.trace(rays, eps=1e-4)
+    np.savez_compressed(os.path.join(HERE, "obj_cornell.npz"), vertices=v, triangles=t, materials=m,
+                        bounds=b, off=o, order=order, rays=rays, **{"hit_" + k: hits[k] for k in hits})
+
+    (v2, t2, m2), cam = scenes.cornell()
+    sc2 = oracle.Scene(v2, t2, m2)
+    params = layouts.default_params(eye_depth_max=8, light_depth_max=8)
+    r = oracle.Renderer(24, 24, 0, params, threads=1)
+    frames = []
+    cache = None
+    for f in range(3):
+        r.render(sc2, cam, 1)
+        frames.append(r.get(0))
+        if f == 0:
+            cache = r.light_cache()
+    np.savez_compressed(os.path.join(HERE, "cornell_frames.npz"), vertices=v2, triangles=t2, materials=m2,
+                        cam=oracle.cam_array(cam), params=params, frames=np.array(frames), cache=cache,
+                        sampleN=r.sample_counts()[0])
+    print("wrote", os.listdir(HERE))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -58,6 +58,7 @@ def lib():
             L.orc_renderer_create.argtypes = [u32, u32, i32, vp, u32]
             L.orc_renderer_destroy.argtypes = [vp]
             L.orc_renderer_set_params.argtypes = [vp, vp]
+            L.orc_renderer_set_window.argtypes = [vp, u32, u32, u32, u32]
             L.orc_render.argtypes = [vp, vp, vp, u32]
             L.orc_renderer_get.argtypes = [vp, i32, vp]
             L.orc_renderer_counts.argtypes = [vp, vp, vp]
@@ -150,6 +151,10 @@ class Renderer:
         if getattr(self, "h", None):
             lib().orc_renderer_destroy(self.h)
             self.h = None
+
+    def set_window(self, x0, y0, full_w, full_h):
+        """Render only the W x H window at (x0, y0) of a full_w x full_h image."""
+        lib().orc_renderer_set_window(self.h, x0, y0, full_w, full_h)
 
     def render(self, scene, cam, frames=1):
         c = cam_array(cam)

@@ -815,8 +815,9 @@ static void trace_pixels(Renderer* r, const Scene& s, const CamF& c, const std::
   parallel_rows(nchunks, r->threads, [&](uint32_t ck) {
     uint32_t e = std::min(n, (ck + 1) * chunk);
     for (uint32_t i = ck * chunk; i < e; i++) {
-      uint32_t pix = pixOf[i], smp = sampleOf[i];
-      uint32_t x = pix % W, y = pix / W;
+      uint32_t smp = sampleOf[i];
+      uint32_t x = pixOf[i] % W + r->x0, y = pixOf[i] / W + r->y0;
+      uint32_t pix = y * (r->fullW ? r->fullW : W) + x;  // global pixel id (RNG stream)
       float u[8];
       draw8(r->p.seed, r->p.request_id, pix, r->frame, kCamera, 0, smp, u);
       V<R> o, d;
@@ -837,8 +838,8 @@ void render_frame(Renderer* r, const Scene& s, const Camera& cam) {
     c.right[k] = right[k];
   }
   c.tanHalf = (float)std::tan((double)(cam.fov * 0.5f));
-  c.W = (float)r->W;
-  c.H = (float)r->H;
+  c.W = (float)(r->fullW ? r->fullW : r->W);
+  c.H = (float)(r->fullH ? r->fullH : r->H);
   float basis9[9] = {cam.pos[0], cam.pos[1], cam.pos[2], cam.dir[0], cam.dir[1], cam.dir[2], up[0], up[1], up[2]};
   bool same = r->started && std::equal(basis9, basis9 + 9, r->camBasis);
   r->frame = same ? r->frame + 1 : 0;

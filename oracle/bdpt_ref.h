@@ -63,6 +63,8 @@ struct Renderer {
   std::vector<LightVertex> cache;
   uint32_t cacheSize = 0;
   uint32_t threads = 1;
+  // sub-window of a larger image (row-band sharding): global pixel = (x+x0, y+y0) of fullW x fullH
+  uint32_t x0 = 0, y0 = 0, fullW = 0, fullH = 0;
   // statistics of the last frame
   uint64_t lastPaths = 0, lastRays = 0, lastNodes = 0, lastTris = 0;
 };

@@ -72,6 +72,13 @@ void* orc_renderer_create(uint32_t W, uint32_t H, int32_t mode, const void* para
   return r;
 }
 void orc_renderer_destroy(void* r) { delete (Renderer*)r; }
+void orc_renderer_set_window(void* rp, uint32_t x0, uint32_t y0, uint32_t fullW, uint32_t fullH) {
+  Renderer* r = (Renderer*)rp;
+  r->x0 = x0;
+  r->y0 = y0;
+  r->fullW = fullW;
+  r->fullH = fullH;
+}
 void orc_renderer_set_params(void* r, const void* params) { ((Renderer*)r)->p = *(const Params*)params; }
 
 // camera: pos[3], dir[3], up[3], fov

@@ -87,6 +87,7 @@ SIGNATURES = {
     "gbpt_attr_set": (i32, [vp, ctypes.c_char_p, f32]),
     "gbpt_gaussian_table": (i32, [f32, u32, vp]),
     "gbpt_bilateral": (i32, [vp, vp, vp, vp, u32, u32, f32, f32, f32, f32, u32, vp, vp, i32]),
+    "gbpt_bilateral_noalloc": (i32, [vp, vp, vp, vp, u32, u32, f32, f32, f32, f32, u32, vp, vp, vp]),
     "gbpt_fmath": (i32, [i32, vp, u32, vp]),
     "gbpt_philox": (i32, [vp, u32, u32, u32, vp]),
 }

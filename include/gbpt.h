@@ -201,6 +201,19 @@ gbpt_status gbpt_gaussian_table(float delta, uint32_t radius, float* g);
 gbpt_status gbpt_bilateral(const float* color, const float* pos, const float* norm, const float* emit,
                            uint32_t width, uint32_t height, float color_eud, float pos_eud, float norm_eud,
                            float emit_eud, uint32_t radius, const float* g, float* out, int32_t is_device);
+/* No counterpart in the reference.  Same filter as gbpt_bilateral on device
+ * arrays, for callers that must not allocate device memory (a process whose
+ * device heap is owned by its own pool, or a latency-critical caller that
+ * cannot afford a cudaMalloc/cudaFree pair): the weight table g (host,
+ * 2*radius+1 floats) is staged in a file-scope device array of 64 floats
+ * instead of a per-call allocation, so radius must be <= 31.  The array is
+ * shared by all calls on a device (calls that overlap on the GPU race on it)
+ * and the first call on a device resolves its address; make that first call
+ * before any stream capture.  stream may be NULL (default stream); the call
+ * returns after the stream has finished the filter. */
+gbpt_status gbpt_bilateral_noalloc(const float* color, const float* pos, const float* norm, const float* emit,
+                                   uint32_t width, uint32_t height, float color_eud, float pos_eud, float norm_eud,
+                                   float emit_eud, uint32_t radius, const float* g, float* out, void* stream);
 
 /* ---- device math, exposed for verification -------------------------------
  * Evaluated by a kernel on host arrays x/out (copied in and out).

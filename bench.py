@@ -26,7 +26,23 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "BDPT Mpaths/s"
-WORKLOAD = "plain streaming BDPT, procedural interior 20x10x30 room + 180 icospheres (57,614 tris), 1024x768, depth 10"
+
+# name -> (scene generator, width, height, mode, depth caps, description)
+WORKLOADS = {
+    "interior": ("interior", 1024, 768, 0, 10,
+                 "plain streaming BDPT, procedural interior 20x10x30 room + 180 icospheres (57,614 tris), "
+                 "1024x768, depth 10"),
+    "hall": ("hall", 1280, 720, 0, 5,
+             "plain streaming BDPT, procedural hall 40x8x40 + 144 pillars + 1200 boxes (332,180 tris), "
+             "1280x720, depth 5"),
+    "hall_adaptive": ("hall", 1280, 720, 1, 5,
+                      "adaptive BDPT + bilateral (radius 4), procedural hall (332,180 tris), 1280x720, depth 5, "
+                      "steady-state budgeted frames"),
+    "cornell": ("cornell", 256, 256, 0, 8,
+                "plain streaming BDPT, Cornell box (36 tris), 256x256, depth 8"),
+}
+WL = WORKLOADS["interior"]
+WORKLOAD = WL[5]
 
 
 def dist_env():
@@ -101,14 +117,16 @@ class ClockSampler:
 
 def scene_and_camera():
     from cudapt_gb300 import scenes
-    return scenes.interior()
+    return getattr(scenes, WL[0])()
 
 
-def params_for(gb_or_layouts):
-    return gb_or_layouts.default_params(eye_depth_max=10, light_depth_max=10)
+def params_for(gb_or_layouts, **kw):
+    extra = dict(filter_radius=4) if WL[3] == 1 else {}
+    extra.update(kw)
+    return gb_or_layouts.default_params(eye_depth_max=WL[4], light_depth_max=WL[4], **extra)
 
 
-W, H = 1024, 768
+W, H = WL[1], WL[2]
 
 
 def run_cpu_sample(threads, rows, frames=1, seed=1234):
@@ -118,10 +136,11 @@ def run_cpu_sample(threads, rows, frames=1, seed=1234):
     from cudapt_gb300 import layouts
     (v, t, m), cam = scene_and_camera()
     sc = oracle.Scene(v, t, m)
-    p = layouts.default_params(eye_depth_max=10, light_depth_max=10, seed=seed)
+    p = params_for(layouts, seed=seed)
     # a band of `rows` full-width rows: same pixels-per-path cost as the full frame
     band_cam = dict(cam)
     r = oracle.Renderer(W, rows, 0, p, threads=threads)
+    r.set_window(0, 0, W, H)
     t0 = time.perf_counter()
     r.render(sc, band_cam, frames)
     dt = time.perf_counter() - t0
@@ -148,9 +167,9 @@ def bench_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "width": W, "height": H, "paths_per_step": W * rows,
-                   "sample": f"1024x{rows} row band per step (full-width rows of the same frame)"},
+                   "sample": f"{W}x{rows} row band per step (full-width rows of the same frame)"},
         "cpu_baseline": {"value": round(v, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
-                         "sample": f"1024x{rows} band x {args.steps} steps, oracle FP32 estimator + restated BVH build "
+                         "sample": f"{W}x{rows} band x {args.steps} steps, oracle FP32 estimator + restated BVH build "
                                    f"({build_s:.2f} s build)"},
         "e2e": {"value": round(v, 4), "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -171,26 +190,31 @@ def bench_gpu(args):
     build_s = scene.build_seconds
     params = params_for(gb)
     np_ = W * H
-    r = gb.RTRenderer(W, H, gb.MODE_BDPT_SC, params)
+    r = gb.RTRenderer(W, H, WL[3], params)
 
     flush = FlushBuffer()
-    # warm-up
-    for _ in range(max(args.warmup, 0)):
+    # warm-up (the adaptive workload first runs its uniform frames, so that
+    # every timed step is a budgeted + filtered frame)
+    warm = max(args.warmup, 0) + (int(params["warmup_frames"]) if WL[3] == 1 else 0)
+    for _ in range(warm):
         r.render_frames(scene, cam, 1, stats=True)
     # timed: one frame per step, L2 flushed (256 MB device memset) before each
     ms = []
-    phases = {"ms_trace": 0.0, "ms_shade": 0.0, "ms_shadow": 0.0, "ms_light": 0.0}
+    phases = {"ms_trace": 0.0, "ms_shade": 0.0, "ms_light": 0.0, "ms_filter": 0.0, "ms_adapt": 0.0,
+              "ms_total": 0.0}
     rays = 0
+    paths = 0
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
             flush()
             st = r.render_frames(scene, cam, 1, stats=True)
             ms.append(st["ms_total"])
             rays += st["rays"]
+            paths += st["paths"]
             for k in phases:
                 phases[k] += st[k]
     total_ms = float(np.sum(ms))
-    value = args.steps * np_ / (total_ms / 1e3) / 1e6
+    value = paths / (total_ms / 1e3) / 1e6
 
     # e2e through the public call with a host result buffer (D2H of the image each step)
     out = np.zeros(np_ * 3, np.float32)
@@ -198,13 +222,13 @@ def bench_gpu(args):
     for _ in range(args.steps):
         r.render(scene, cam, stats=False)
     e2e_s = time.perf_counter() - t0
-    e2e = args.steps * np_ / e2e_s / 1e6
+    e2e = paths / e2e_s / 1e6
 
     # work counters for the roofline (separate, untimed frame)
     r.set_counting(True)
     cst = r.render_frames(scene, cam, 1, stats=True)
     r.set_counting(False)
-    trace_bytes = 40 * cst["nodes"] + 48 * cst["tris"]
+    trace_bytes = 40 * (cst["nodes"] + cst["shadow_nodes"]) + 48 * (cst["tris"] + cst["shadow_tris"])
     trace_ms = cst["ms_trace"]
     achieved = trace_bytes / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else None
     peak, peak_kind = load_peaks()
@@ -215,9 +239,13 @@ def bench_gpu(args):
         rows = int(os.environ.get("GBPT_CPU_ROWS", "24"))
         p, dt, bs = run_cpu_sample(threads, rows)
         cpu = {"value": round(p / dt / 1e6, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
-               "sample": f"1024x{rows} row band of one frame, oracle FP32 estimator ({bs:.2f} s restated BVH build)"}
+               "sample": f"{W}x{rows} row band of one uniform frame, oracle FP32 estimator "
+                         f"({bs:.2f} s restated BVH build)"}
 
-    launches_per_frame = 1 + 3 * int(params["eye_depth_max"]) + 1
+    D = int(params["eye_depth_max"])
+    # camera + D x (walk, shade) + final walk + apply; budgeted frames: filter +
+    # 6 budget kernels + D x (walk, shade) + final walk + accumulate
+    launches_per_frame = 2 * D + 3 if WL[3] == 0 else 2 * D + 9
     light_frames = sum(1 for f in range(args.warmup, args.warmup + args.steps)
                        if f % int(params["light_every"]) == 0)
     line = {
@@ -226,14 +254,14 @@ def bench_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (procedural scene, seeded)",
         "config": {"workload": WORKLOAD, "width": W, "height": H, "paths_per_step": np_,
-                   "eye_depth_max": 10, "light_depth_max": 10, "tris": int(len(t)),
+                   "eye_depth_max": D, "light_depth_max": D, "tris": int(len(t)),
                    "l2": "flushed before every timed step (256 MB device memset)",
                    "bvh_build_s": round(build_s, 4), "rays_per_s": round(rays / (total_ms / 1e3), 1),
                    "phase_ms_per_step": {k: round(v_ / args.steps, 4) for k, v_ in phases.items()},
                    "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": round(e2e * world, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": 40,
                 "d2h_bytes_per_step": np_ * 12},
-        "roofline": {"bound": "hbm", "kernel": "k_trace (closest-hit BVH walk)",
+        "roofline": {"bound": "hbm", "kernel": "k_walk (closest-hit + shadow BVH walks)",
                      "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4) if achieved else None, "peak_kind": peak_kind,
                      "traffic": None,
@@ -266,7 +294,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbpt", choices=["gbpt", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="interior", choices=sorted(WORKLOADS))
     args = ap.parse_args()
+    global WL, WORKLOAD, W, H
+    WL = WORKLOADS[args.workload]
+    WORKLOAD, W, H = WL[5], WL[1], WL[2]
     if args.impl == "reference":
         bench_reference(args)
     else:

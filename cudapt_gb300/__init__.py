@@ -11,12 +11,12 @@ import numpy as np
 
 from . import layouts
 from ._native import GbptError, Stats, as_c, check, load, ptr
-from .layouts import (MATERIAL, MODE_BDPT_SC, MODE_BDPT_SC_ADAP_BILAT, PARAMS, TRIANGLE, VERTEX,
-                      default_params, material)
+from .layouts import (MATERIAL, MODE_BDPT_SC, MODE_BDPT_SC_ADAP_BILAT, MODE_BDPT_SC_ADAP_BILAT_BINARY, PARAMS,
+                      TRIANGLE, VERTEX, default_params, material)
 
 __all__ = [
     "RTScene", "RTRenderer", "GbptError", "default_params", "material", "layouts",
-    "MODE_BDPT_SC", "MODE_BDPT_SC_ADAP_BILAT", "VERTEX", "TRIANGLE", "MATERIAL", "PARAMS",
+    "MODE_BDPT_SC", "MODE_BDPT_SC_ADAP_BILAT", "MODE_BDPT_SC_ADAP_BILAT_BINARY", "VERTEX", "TRIANGLE", "MATERIAL", "PARAMS",
     "device_available", "camera",
 ]
 
@@ -117,7 +117,7 @@ class RTRenderer:
     def __init__(self, width, height, mode=MODE_BDPT_SC, params=None):
         L = load()
         self.width, self.height = int(width), int(height)
-        p = default_params() if params is None else np.array(params, PARAMS)
+        p = layouts.as_params(params)
         h = ctypes.c_void_p()
         check(L.gbpt_renderer_create(self.width, self.height, int(mode), ptr(p), ctypes.addressof(h)))
         self._h = h
@@ -155,7 +155,7 @@ class RTRenderer:
 
     @params.setter
     def params(self, p):
-        p = np.array(p, PARAMS)
+        p = layouts.as_params(p)
         check(load().gbpt_set_params(self._h, ptr(p)))
 
     def close(self):

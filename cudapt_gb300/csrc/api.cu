@@ -7,6 +7,7 @@
 // and renderer owns its buffers, and a renderer owns its CUDA stream.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -192,17 +193,31 @@ struct gbpt_renderer {
   float gaussKey[2] = {-1.f, -1.f};
   std::vector<std::pair<int, cudaEvent_t>> evs;
   std::vector<cudaEvent_t> evPool;
+  // light passes run one group ahead on a side stream into the cache the
+  // current frames do not read; tag = (epoch, frame) the cache was made for
+  cudaStream_t stLight = nullptr;
+  cudaEvent_t evMain = nullptr, evLight[2] = {nullptr, nullptr};
+  bool lightPending[2] = {false, false};
+  uint64_t epoch = 0;
+  uint64_t cacheEpoch[2] = {~0ull, ~0ull};
+  uint32_t cacheFrame[2] = {0, 0};
+  uint32_t lastSel = 0;
 
   void free_dev() {
     for (int k = 0; k < 2; k++) rb.wave[k] = Wave{};
     dfree(waveMem);
     dfree(rb.hit);
-    dfree(rb.sh);
+    dfree(rb.sh[0]);
+    dfree(rb.sh[1]);
     dfree(rb.res);
     dfree(rb.gbuf);
     dfree(rb.slotPix);
     dfree(rb.slotSmp);
-    dfree(rb.cache);
+    if (stLight) cudaStreamSynchronize(stLight);
+    dfree(rb.cache[0]);
+    dfree(rb.cache[1]);
+    cacheEpoch[0] = cacheEpoch[1] = ~0ull;
+    lightPending[0] = lightPending[1] = false;
     dfree(rb.ctr);
     dfree(ab.err);
     dfree(ab.cnt);
@@ -210,6 +225,7 @@ struct gbpt_renderer {
     dfree(ab.blockSum);
     dfree(ab.partial);
     dfree(ab.filtered);
+    dfree(ab.coop);
     dfree(result);
     dfree(gpos);
     dfree(gnorm);
@@ -222,6 +238,9 @@ struct gbpt_renderer {
     if (st) cudaStreamSynchronize(st);
     free_dev();
     for (auto e : evPool) cudaEventDestroy(e);
+    for (cudaEvent_t e : {evMain, evLight[0], evLight[1]})
+      if (e) cudaEventDestroy(e);
+    if (stLight) cudaStreamDestroy(stLight);
     if (st) cudaStreamDestroy(st);
   }
 };
@@ -245,7 +264,7 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   const size_t cap = np;
   const uint32_t cacheCap = std::max(1u, r->p.light_paths * (1 + r->p.light_depth_max));
   // admission: refuse when the buffers cannot fit in free HBM
-  size_t need = cap * (128 + 16 + 48 + 16 + 48 + 8) + np * (12 * 5 + 4 + 4 * 4) + (size_t)cacheCap * 96;
+  size_t need = cap * (128 + 16 + 96 + 16 + 48 + 8) + np * (12 * 5 + 4 + 4 * 4) + (size_t)cacheCap * 192;
   size_t freeB = 0, totB = 0;
   CK(cudaMemGetInfo(&freeB, &totB));
   if (need + (64ull << 20) > freeB)
@@ -257,15 +276,18 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
     r->rb.wave[k] = Wave{b, b + cap, b + 2 * cap, b + 3 * cap};
   }
   CK(dalloc(&r->rb.hit, cap));
-  CK(dalloc(&r->rb.sh, cap * 3));
+  CK(dalloc(&r->rb.sh[0], cap * 3));
+  CK(dalloc(&r->rb.sh[1], cap * 3));
   CK(dalloc(&r->rb.res, cap));
   CK(dalloc(&r->rb.gbuf, cap * 3));
   CK(dalloc(&r->rb.slotPix, cap));
   CK(dalloc(&r->rb.slotSmp, cap));
-  CK(dalloc(&r->rb.cache, (size_t)cacheCap * 6));
+  CK(dalloc(&r->rb.cache[0], (size_t)cacheCap * 6));
+  CK(dalloc(&r->rb.cache[1], (size_t)cacheCap * 6));
   CK(dalloc(&r->rb.ctr, 1));
   CK(cudaMemsetAsync(r->rb.ctr, 0, sizeof(DevCounters), r->st));
-  CK(cudaMemsetAsync(r->rb.cache, 0, (size_t)cacheCap * 96, r->st));
+  CK(cudaMemsetAsync(r->rb.cache[0], 0, (size_t)cacheCap * 96, r->st));
+  CK(cudaMemsetAsync(r->rb.cache[1], 0, (size_t)cacheCap * 96, r->st));
   r->rb.cap = (uint32_t)cap;
   r->rb.cacheCap = cacheCap;
   CK(dalloc(&r->result, np * 3));
@@ -280,6 +302,8 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   CK(dalloc(&r->ab.blockSum, adapt_scan_blocks((uint32_t)np)));
   CK(dalloc(&r->ab.partial, adapt_reduce_blocks((uint32_t)np)));
   CK(dalloc(&r->ab.filtered, np * 3));
+  CK(dalloc(&r->ab.coop, kCoopWords));
+  CK(cudaMemsetAsync(r->ab.coop, 0, kCoopWords * 4, r->st));
   for (float* b : {r->result, r->gpos, r->gnorm, r->gdiff, r->ab.filtered})
     CK(cudaMemsetAsync(b, 0, np * 12, r->st));
   CK(cudaMemsetAsync(r->sampleN, 0, np * 4, r->st));
@@ -332,6 +356,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
                      cam->dir[2], up[0],       up[1],       up[2]};
   bool same = r->started && r->sceneVersion == s->version && std::memcmp(basis9, r->camBasis, sizeof(basis9)) == 0;
   r->frame = same ? r->frame + 1 : 0;
+  if (!same) r->epoch++;  // light passes made ahead for the old sequence are stale
   std::memcpy(r->camBasis, basis9, sizeof(basis9));
   r->started = true;
   r->sceneVersion = s->version;
@@ -356,17 +381,47 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   a.lightPaths = r->p.light_paths;
   for (int k = 0; k < 3; k++) a.env[k] = r->p.env[k];
   a.useEnv = (r->p.env[0] != 0.f || r->p.env[1] != 0.f || r->p.env[2] != 0.f) ? 1u : 0u;
-  const bool adaptive = r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT;
-  a.specPush = adaptive ? 1u : 0u;
+  const bool adaptive = r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT || r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY;
+  const bool binary = r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY;
+  // the PLL variant pushes the specular origin along reflDir (AdapBilatAtomic.cu:583); the others do not
+  a.specPush = r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT ? 1u : 0u;
   a.gbuffer = adaptive ? 1u : 0u;
   a.counting = r->counting ? 1u : 0u;
   const DevScene& S = s->dev;
   cudaStream_t st = r->st;
 
   mark(r, kPhOther, timing);
-  if (r->frame % r->p.light_every == 0) {
-    CK(launch_light_pass(S, a, r->rb, st));
-    mark(r, kPhLight, timing);
+  // light pass (src/cudaRTBDPTStream.cu:875-906): group g = frame / light_every
+  // reads cache g % 2.  Its light pass normally ran ahead on the side stream;
+  // if not (first group, camera change), it runs here on the main stream.
+  const uint32_t k = r->p.light_every;
+  const uint32_t g = r->frame / k;
+  const uint32_t sel = g & 1u;
+  a.cacheSel = sel;
+  r->lastSel = sel;
+  if (r->frame % k == 0) {
+    const bool ready = r->cacheEpoch[sel] == r->epoch && r->cacheFrame[sel] == r->frame;
+    if (r->lightPending[sel]) CK(cudaStreamWaitEvent(st, r->evLight[sel], 0));
+    r->lightPending[sel] = false;
+    if (!ready) {
+      CK(launch_light_pass(S, a, r->rb, st));
+      r->cacheEpoch[sel] = r->epoch;
+      r->cacheFrame[sel] = r->frame;
+      mark(r, kPhLight, timing);
+    }
+    // run the next group's light pass ahead, into the other cache: it waits
+    // for everything queued so far (earlier frames that read that cache)
+    const uint32_t nsel = sel ^ 1u;
+    CK(cudaEventRecord(r->evMain, st));
+    CK(cudaStreamWaitEvent(r->stLight, r->evMain, 0));
+    FrameArgs an = a;
+    an.frame = r->frame + k;
+    an.cacheSel = nsel;
+    CK(launch_light_pass(S, an, r->rb, r->stLight));
+    CK(cudaEventRecord(r->evLight[nsel], r->stLight));
+    r->lightPending[nsel] = true;
+    r->cacheEpoch[nsel] = r->epoch;
+    r->cacheFrame[nsel] = r->frame + k;
   }
   const bool budgeted = adaptive && r->frame >= r->p.warmup_frames;
   if (budgeted) {
@@ -382,24 +437,42 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
                         r->p.filter_color_eud, r->p.filter_pos_eud, r->p.filter_norm_eud, r->p.filter_diff_eud,
                         r->p.filter_radius, r->gauss, r->ab.filtered, st));
     mark(r, kPhFilter, timing);
-    CK(launch_adapt_budget(a, r->rb, r->ab, r->result, r->sampleN, r->p.desired_n, st));
+    if (binary)
+      CK(launch_binary_budget(a, r->rb, r->ab, r->result, r->sampleN, r->p.desired_n, r->p.min_trace_prob, st));
+    else
+      CK(launch_adapt_budget(a, r->rb, r->ab, r->result, r->sampleN, r->p.desired_n, st));
     mark(r, kPhAdapt, timing);
   } else {
     CK(launch_camera(a, r->rb, st));
     mark(r, kPhOther, timing);
   }
+  // bounce d < K: walk (extension rays of d + shadow rays of d-1), then shade
+  // d, one launch each; bounces >= K: one persistent kernel per frame carries
+  // every remaining path to its end (few paths are left by then, and per-bounce
+  // launches would each wait for their slowest ray)
   int in = 0;
-  for (uint32_t d = 0; d < r->p.eye_depth_max; d++) {
-    CK(launch_trace(S, a, r->rb, in, st));
+  const uint32_t D = r->p.eye_depth_max;
+  const uint32_t K = std::min(tail_from(D), D);
+  for (uint32_t d = 0; d < K; d++) {
+    CK(launch_walk(S, a, r->rb, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), st));
     mark(r, kPhTrace, timing);
-    CK(launch_shade(S, a, r->rb, in, d, st));
+    CK(launch_shade(S, a, r->rb, in, d, K < D && d + 1 == K, st));
     mark(r, kPhShade, timing);
-    CK(launch_shadow(S, a, r->rb, st));
-    mark(r, kPhShadow, timing);
     in ^= 1;
   }
+  if (K < D) {
+    CK(launch_tail(S, a, r->rb, in, K > 0 ? (int)((K - 1) & 1u) : -1, K, st));
+  } else {
+    // shadow rays of the last bounce (none in practice: paths at the depth cap
+    // terminate without connecting; kept so the sequence needs no special case)
+    CK(launch_walk(S, a, r->rb, -1, (int)((D - 1) & 1u), (int)(D & 1u), st));
+  }
+  mark(r, kPhTrace, timing);
   if (budgeted) {
-    CK(launch_adapt_accum(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
+    if (binary)
+      CK(launch_binary_apply(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
+    else
+      CK(launch_adapt_accum(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
     mark(r, kPhAdapt, timing);
   } else {
     CK(launch_apply(a, r->rb, r->result, r->sampleN, adaptive ? r->gpos : nullptr, r->gnorm, r->gdiff, st));
@@ -438,18 +511,27 @@ gbpt_status render_impl(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam,
   }
   const size_t np = (size_t)r->W * r->H;
   if (out) {
-    const float* src = (r->debugMode == 4.f && r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT) ? r->ab.filtered : r->result;
+    const float* src = (r->debugMode == 4.f && r->mode != GBPT_MODE_BDPT_SC) ? r->ab.filtered : r->result;
     CK(cudaMemcpyAsync(out, src, np * 12, outDev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, r->st));
   }
   CK(cudaStreamSynchronize(r->st));
   CK(cudaGetLastError());
+  {  // device-side error words (bounded waits, bounds checks): report once, then clear
+    uint32_t flags = 0;
+    CK(cudaMemcpy(&flags, &r->rb.ctr->errFlags, 4, cudaMemcpyDeviceToHost));
+    if (flags) {
+      CK(cudaMemset(&r->rb.ctr->errFlags, 0, 4));
+      if (flags & 4u) return fail(GBPT_ERR_TIMEOUT, "grid barrier of the binary allocator timed out");
+      return fail(GBPT_ERR_BOUNDS, "device bounds check tripped (light cache)");
+    }
+  }
   if (timing) {
     DevCounters after{};
     stt = read_ctr(r, &after);
     if (stt != GBPT_OK) return stt;
     std::memset(stats, 0, sizeof(*stats));
     stats->frame = r->frame;
-    stats->light_vertices = after.cacheSize;
+    stats->light_vertices = after.cacheSize[r->lastSel];
     stats->paths = after.paths;
     stats->rays = after.rays - before.rays;
     stats->nodes = after.nodes - before.nodes;
@@ -470,7 +552,6 @@ gbpt_status render_impl(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam,
     stats->ms_shadow = ph[kPhShadow];
     stats->ms_filter = ph[kPhFilter];
     stats->ms_adapt = ph[kPhAdapt];
-    if (after.errFlags) return fail(GBPT_ERR_BOUNDS, "device bounds check tripped (light cache)");
   }
   return GBPT_OK;
 }
@@ -496,6 +577,7 @@ const AttrDef kAttrs[] = {
     {"Warmup Frames", 1, offsetof(gbpt_params, warmup_frames)},
     {"Filter Sigma Spatial", 0, offsetof(gbpt_params, filter_sigma_spatial)},
     {"Seed", 1, offsetof(gbpt_params, seed)},
+    {"Min Trace Probability", 0, offsetof(gbpt_params, min_trace_prob)},
 };
 constexpr uint32_t kAttrN = sizeof(kAttrs) / sizeof(kAttrs[0]);
 
@@ -541,6 +623,7 @@ gbpt_status gbpt_params_default(gbpt_params* p) {
   p->filter_diffuse = 0;
   p->filter_sigma_spatial = 0.f;
   p->request_id = 0;
+  p->min_trace_prob = 0.f;
   return GBPT_OK;
 }
 
@@ -679,7 +762,7 @@ gbpt_status gbpt_renderer_create(uint32_t width, uint32_t height, int32_t mode, 
   *out = nullptr;
   if (width == 0 || height == 0 || (uint64_t)width * height > (1ull << 26))
     return fail(GBPT_ERR_INVALID_ARG, "image size must be 1..2^26 pixels");
-  if (mode != GBPT_MODE_BDPT_SC && mode != GBPT_MODE_BDPT_SC_ADAP_BILAT)
+  if (mode < GBPT_MODE_BDPT_SC || mode > GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY)
     return fail(GBPT_ERR_INVALID_ARG, "unknown renderer mode");
   gbpt_params p;
   if (params) {
@@ -695,7 +778,13 @@ gbpt_status gbpt_renderer_create(uint32_t width, uint32_t height, int32_t mode, 
   r->H = height;
   r->mode = mode;
   r->p = p;
+  int prLow = 0, prHigh = 0;
+  cudaDeviceGetStreamPriorityRange(&prLow, &prHigh);
   cudaError_t e = cudaStreamCreateWithFlags(&r->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&r->stLight, cudaStreamNonBlocking, prLow);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->evMain, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->evLight[0], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->evLight[1], cudaEventDisableTiming);
   if (e != cudaSuccess) {
     delete r;
     return fail(GBPT_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
@@ -711,7 +800,7 @@ gbpt_status gbpt_renderer_destroy(gbpt_renderer* r) {
 
 gbpt_status gbpt_set_mode(gbpt_renderer* r, int32_t mode) {
   if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
-  if (mode != GBPT_MODE_BDPT_SC && mode != GBPT_MODE_BDPT_SC_ADAP_BILAT)
+  if (mode < GBPT_MODE_BDPT_SC || mode > GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY)
     return fail(GBPT_ERR_INVALID_ARG, "unknown renderer mode");
   if (mode != r->mode) {
     r->mode = mode;
@@ -778,12 +867,13 @@ gbpt_status gbpt_read_buffer(gbpt_renderer* r, int32_t which, void* dst, size_t 
       DevCounters c{};
       gbpt_status st = read_ctr(r, &c);
       if (st != GBPT_OK) return st;
-      need = (size_t)c.cacheSize * 21 * 4;
+      const uint32_t cs = c.cacheSize[r->lastSel];
+      need = (size_t)cs * 21 * 4;
       if (bytes < need) return fail(GBPT_ERR_INVALID_ARG, "destination too small");
-      std::vector<float4> raw((size_t)c.cacheSize * 6);
-      if (c.cacheSize) CK(cudaMemcpy(raw.data(), r->rb.cache, raw.size() * 16, cudaMemcpyDeviceToHost));
-      std::vector<float> o((size_t)c.cacheSize * 21);
-      for (uint32_t i = 0; i < c.cacheSize; i++) {
+      std::vector<float4> raw((size_t)cs * 6);
+      if (cs) CK(cudaMemcpy(raw.data(), r->rb.cache[r->lastSel], raw.size() * 16, cudaMemcpyDeviceToHost));
+      std::vector<float> o((size_t)cs * 21);
+      for (uint32_t i = 0; i < cs; i++) {
         const float4* q = &raw[(size_t)i * 6];
         float* d = &o[(size_t)i * 21];
         const float4* fields[6] = {&q[0], &q[1], &q[2], &q[3], &q[4], &q[5]};

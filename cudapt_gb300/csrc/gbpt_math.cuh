@@ -177,7 +177,7 @@ GB_HD u4 philox(u4 ctr, uint32_t k0, uint32_t k1) {
 // 23 random bits -> (2m+1) * 2^-24 in (0, 1), exact
 GB_HD float u01(uint32_t x) { return (float)(x >> 9) * 0x1p-23f + 0x1p-24f; }
 
-enum Stream : uint32_t { kCamera = 0, kEyeBounce = 1, kLightGen = 2, kLightBounce = 3 };
+enum Stream : uint32_t { kCamera = 0, kEyeBounce = 1, kLightGen = 2, kLightBounce = 3, kBinaryAccept = 4 };
 
 // Eight uniforms for one (path, frame, stream, depth, sample): two Philox blocks.
 GB_HD void draw8(uint32_t k0, uint32_t k1, uint32_t path, uint32_t frame, uint32_t stream, uint32_t depth,

@@ -233,6 +233,7 @@ __global__ void k_scan_blocks(uint32_t* blockSum, uint32_t nb, uint32_t gen, Dev
     unsigned long long tot = carry < gen ? carry : gen;
     ctr->wave[0] = (uint32_t)tot;
     ctr->paths = (uint32_t)tot;
+    ctr->fetchT = 0;
   }
 }
 
@@ -293,28 +294,42 @@ __global__ void k_gen_adapt(FrameArgs a, RenderBuffers b, const uint32_t* __rest
   }
 }
 
-// ordered per-pixel sums, then the running means
+// Per-pixel sums of the budgeted samples, then the running means.  One warp
+// per pixel: lane l adds samples l, l+32, l+64, ... in slot order, then the
+// 32 partial sums are combined by a butterfly (x += shfl_xor(x, m) for
+// m = 16, 8, 4, 2, 1).  The order is a fixed function of the sample count, so
+// the result does not depend on timing, and a pixel with thousands of
+// samples costs one warp pass instead of a serial loop.
+__device__ __forceinline__ float bfly(float v) {
+  for (int m = 16; m > 0; m >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, m);
+  return v;
+}
+
 __global__ void k_accum(FrameArgs a, RenderBuffers b, const uint32_t* __restrict__ off,
                         const uint32_t* __restrict__ cnt, float* result, uint32_t* sampleN, float* gpos,
                         float* gnorm, float* gdiff) {
   const uint32_t np = a.width * a.height;
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= np) return;
-  float tr[3] = {0.f, 0.f, 0.f}, tp[3] = {0.f, 0.f, 0.f}, tn[3] = {0.f, 0.f, 0.f}, td[3] = {0.f, 0.f, 0.f};
+  const uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  if (p >= np) return;  // warp-uniform
+  float v[12] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   uint32_t tN = 0;
   const uint32_t o = off[p], c = cnt[p];
-  for (uint32_t s = o; s < o + c; s++) {
+  for (uint32_t s = o + lane; s < o + c; s += 32) {
     float4 r = b.res[s];
     if (isinf(r.x) || isinf(r.y) || isinf(r.z)) continue;
     uint32_t n = __float_as_uint(r.w);
     float fn = (float)n;
     float4 g0 = b.gbuf[3 * (size_t)s], g1 = b.gbuf[3 * (size_t)s + 1], g2 = b.gbuf[3 * (size_t)s + 2];
-    tr[0] = tr[0] + r.x; tr[1] = tr[1] + r.y; tr[2] = tr[2] + r.z;
-    tp[0] = tp[0] + g0.x * fn; tp[1] = tp[1] + g0.y * fn; tp[2] = tp[2] + g0.z * fn;
-    tn[0] = tn[0] + g1.x * fn; tn[1] = tn[1] + g1.y * fn; tn[2] = tn[2] + g1.z * fn;
-    td[0] = td[0] + g2.x * fn; td[1] = td[1] + g2.y * fn; td[2] = td[2] + g2.z * fn;
+    v[0] = v[0] + r.x; v[1] = v[1] + r.y; v[2] = v[2] + r.z;
+    v[3] = v[3] + g0.x * fn; v[4] = v[4] + g0.y * fn; v[5] = v[5] + g0.z * fn;
+    v[6] = v[6] + g1.x * fn; v[7] = v[7] + g1.y * fn; v[8] = v[8] + g1.z * fn;
+    v[9] = v[9] + g2.x * fn; v[10] = v[10] + g2.y * fn; v[11] = v[11] + g2.z * fn;
     tN += n;
   }
+  for (int k = 0; k < 12; k++) v[k] = bfly(v[k]);
+  for (int m = 16; m > 0; m >>= 1) tN += __shfl_xor_sync(0xffffffffu, tN, m);
+  if (lane != 0) return;
   float* q = result + 3 * (size_t)p;
   float* P = gpos + 3 * (size_t)p;
   float* Nn = gnorm + 3 * (size_t)p;
@@ -328,14 +343,233 @@ __global__ void k_accum(FrameArgs a, RenderBuffers b, const uint32_t* __restrict
   if (nn > N) {
     const float rInf = 1.f / (float)nn, oInf = (float)N * rInf;
     for (int k = 0; k < 3; k++) {
-      q[k] = fmaxf(rInf * tr[k] + oInf * q[k], 0.f);
-      P[k] = rInf * tp[k] + oInf * P[k];
-      Nn[k] = rInf * tn[k] + oInf * Nn[k];
-      Dd[k] = rInf * td[k] + oInf * Dd[k];
+      q[k] = fmaxf(rInf * v[k] + oInf * q[k], 0.f);
+      P[k] = rInf * v[3 + k] + oInf * P[k];
+      Nn[k] = rInf * v[6 + k] + oInf * Nn[k];
+      Dd[k] = rInf * v[9 + k] + oInf * Dd[k];
     }
     N = nn;
   }
   sampleN[p] = N;
+}
+
+// ---------------------------------------------------------------------------
+// Binary allocator.  The reference runs its window search as a host loop
+// with a D2H count per pass; here one cooperative kernel (all blocks
+// resident) runs every pass, separated by a grid barrier.  The barrier spins
+// on a generation word with an iteration limit: on timeout it sets bit 2 of
+// DevCounters::errFlags and the kernel returns (the host reports
+// GBPT_ERR_TIMEOUT).
+// coop layout: [0] barrier count, [1] barrier generation, [2] passes,
+// [16, 16+G) per-block values, [4096, 4096+80) paths per pass.
+constexpr uint32_t kCoopBlocks = 16, kCoopPass = 4096, kMaxPasses = 64;
+constexpr unsigned long long kBarrierSpins = 1ull << 24;
+
+__device__ __forceinline__ bool grid_barrier(uint32_t* coop, uint32_t nblocks, DevCounters* ctr) {
+  __shared__ uint32_t ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile uint32_t* gen = coop + 1;
+    const uint32_t g = *gen;
+    __threadfence();
+    const uint32_t arrived = atomicAdd(coop, 1u);
+    ok = 1u;
+    if (arrived == nblocks - 1) {
+      coop[0] = 0;
+      __threadfence();
+      atomicAdd(coop + 1, 1u);
+    } else {
+      unsigned long long spins = 0;
+      while (*gen == g) {
+        if (++spins > kBarrierSpins) {
+          atomicOr(&ctr->errFlags, 4u);
+          ok = 0u;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0u;
+}
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* ws) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  uint32_t t = 0;
+  for (uint32_t w = 0; w < (blockDim.x + 31) / 32; w++) t += ws[w];
+  return t;
+}
+
+__device__ __forceinline__ bool bin_accept(const FrameArgs& a, const float* err, uint32_t p, uint32_t pass, float mid,
+                                           float minProb) {
+  gb::u4 r = gb::philox(gb::u4{p, a.frame, (uint32_t)gb::kBinaryAccept << 24, pass}, a.key0, a.key1);
+  return !(gb::u01(r.a) * mid > fmaxf(err[p], minProb));
+}
+
+__global__ void __launch_bounds__(256) k_bin_search(FrameArgs a, RenderBuffers b, const float* __restrict__ err,
+                                                    uint32_t np, uint32_t D, float minProb, uint32_t* coop) {
+  __shared__ uint32_t ws[32];
+  __shared__ float wf[32];
+  const uint32_t G = gridDim.x;
+  const uint32_t per = (np + G - 1) / G;
+  const uint32_t lo = min(np, blockIdx.x * per), hi = min(np, lo + per);
+  uint32_t* blockVal = coop + kCoopBlocks;
+  uint32_t* passLen = coop + kCoopPass;
+  // max error (NaN ignored, as the reference's thrust::maximum from 0)
+  float m = 0.f;
+  for (uint32_t p = lo + threadIdx.x; p < hi; p += blockDim.x) m = fmaxf(m, err[p]);
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) wf[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (uint32_t w = 0; w < (blockDim.x + 31) / 32; w++) t = fmaxf(t, wf[w]);
+    blockVal[blockIdx.x] = __float_as_uint(t);
+  }
+  if (!grid_barrier(coop, G, b.ctr)) return;
+  float maxE = 0.f;
+  for (uint32_t k = 0; k < G; k++) maxE = fmaxf(maxE, __uint_as_float(((volatile uint32_t*)blockVal)[k]));
+  float left = 0.f, right = maxE * 2.f;
+  const float desired = (float)np / (float)D;
+  uint32_t accum = 0, passes = 0;
+  if (!grid_barrier(coop, G, b.ctr)) return;  // every block has read blockVal
+  for (uint32_t pass = 0; accum < np && pass < kMaxPasses; pass++) {
+    const float mid = (left + right) * 0.5f;
+    uint32_t c = 0;
+    for (uint32_t p = lo + threadIdx.x; p < hi; p += blockDim.x) c += bin_accept(a, err, p, pass, mid, minProb) ? 1u : 0u;
+    c = block_sum(c, ws);
+    if (threadIdx.x == 0) blockVal[blockIdx.x] = c;
+    if (!grid_barrier(coop, G, b.ctr)) return;
+    uint32_t total = 0, before = 0;
+    for (uint32_t k = 0; k < G; k++) {
+      const uint32_t v = ((volatile uint32_t*)blockVal)[k];
+      if (k < blockIdx.x) before += v;
+      total += v;
+    }
+    const uint32_t take = min(np - accum, total);
+    // write accepted pixels of this block in pixel order (stable compaction)
+    uint32_t rank = before;
+    for (uint32_t base = lo; base < hi; base += blockDim.x) {
+      const uint32_t p = base + threadIdx.x;
+      const bool acc = p < hi && bin_accept(a, err, p, pass, mid, minProb);
+      const uint32_t bal = __ballot_sync(0xffffffffu, acc);
+      uint32_t lm;
+      asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lm));
+      __syncthreads();
+      if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = __popc(bal);
+      __syncthreads();
+      uint32_t wbefore = 0, tile = 0;
+      for (uint32_t w = 0; w < (blockDim.x + 31) / 32; w++) {
+        if (w < (threadIdx.x >> 5)) wbefore += ws[w];
+        tile += ws[w];
+      }
+      if (acc) {
+        const uint32_t r = rank + wbefore + __popc(bal & lm);
+        if (r < take) {
+          b.slotPix[accum + r] = p;
+          b.slotSmp[accum + r] = pass;
+        }
+      }
+      rank += tile;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) passLen[pass] = take;
+    accum += take;
+    passes = pass + 1;
+    if (!grid_barrier(coop, G, b.ctr)) return;  // blockVal is reused by the next pass
+    if (take == 0) break;
+    if ((float)take < desired)
+      right = mid;
+    else if ((float)take > desired)
+      left = mid;
+  }
+  if (accum < np) {  // leftover slots: pixel ids 0, 1, ... (pt_fillTempAdapPathQueue_kernel)
+    const uint32_t fill = np - accum;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < fill; k += G * blockDim.x) {
+      b.slotPix[accum + k] = k;
+      b.slotSmp[accum + k] = passes;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) passLen[passes] = fill;
+    passes++;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    coop[2] = passes;
+    b.ctr->wave[0] = np;
+    b.ctr->paths = np;
+    b.ctr->fetchT = 0;
+  }
+}
+
+// camera path for queue entry s (pixel slotPix[s], sample slotSmp[s])
+__global__ void k_gen_queue(FrameArgs a, RenderBuffers b, uint32_t np) {
+  using namespace gb;
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= np) return;
+  const uint32_t p = b.slotPix[s], k = b.slotSmp[s];
+  const uint32_t x = p % a.width, y = p / a.width;
+  float u[4];
+  draw4(a.key0, a.key1, p, a.frame, kCamera, 0, k, 0, u);
+  const float W = a.W, H = a.H, th = a.tanHalf;
+  float cu = ((((2.f * ((float)x + 0.5f)) / W) - 1.f) * th * W) / H;
+  float cv = (((2.f * ((float)y + 0.5f)) / H) - 1.f) * th;
+  float au = cu + ((u[0] - 0.5f) / H) * th;
+  float av = cv + ((u[1] - 0.5f) / H) * th;
+  f3 dir = normalize((mk(a.camRight[0], a.camRight[1], a.camRight[2]) * au +
+                      mk(a.camUp[0], a.camUp[1], a.camUp[2]) * av) +
+                     mk(a.camDir[0], a.camDir[1], a.camDir[2]));
+  Wave w = b.wave[0];
+  w.o[s] = make_float4(a.camPos[0], a.camPos[1], a.camPos[2], __uint_as_float(s));
+  w.d[s] = make_float4(dir.x, dir.y, dir.z, __uint_as_float(p));
+  w.thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
+  w.smp[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  b.res[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  b.gbuf[3 * (size_t)s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  b.gbuf[3 * (size_t)s + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+  b.gbuf[3 * (size_t)s + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// running means, pass by pass (a pixel appears at most once per pass)
+__global__ void __launch_bounds__(256) k_bin_apply(FrameArgs a, RenderBuffers b, uint32_t* coop, float* result,
+                                                   uint32_t* sampleN, float* gpos, float* gnorm, float* gdiff) {
+  const uint32_t G = gridDim.x;
+  const uint32_t passes = coop[2];
+  const uint32_t* passLen = coop + kCoopPass;
+  float* planes[3] = {gpos, gnorm, gdiff};
+  uint32_t start = 0;
+  for (uint32_t c = 0; c < passes; c++) {
+    const uint32_t len = passLen[c];
+    for (uint32_t s = start + blockIdx.x * blockDim.x + threadIdx.x; s < start + len; s += G * blockDim.x) {
+      const uint32_t p = b.slotPix[s];
+      const float4 r = b.res[s];
+      const uint32_t n = __float_as_uint(r.w);
+      if (n == 0) continue;
+      if (a.frame == 0) sampleN[p] = 0;
+      const uint32_t old = sampleN[p];
+      const uint32_t nn = old + n;
+      if (!(nn > old)) continue;
+      if (isinf(r.x) || isinf(r.y) || isinf(r.z)) continue;
+      const float rInf = 1.f / (float)nn, oInf = (float)old * rInf;
+      float* q = result + 3 * (size_t)p;
+      q[0] = fmaxf(rInf * r.x + oInf * q[0], 0.f);
+      q[1] = fmaxf(rInf * r.y + oInf * q[1], 0.f);
+      q[2] = fmaxf(rInf * r.z + oInf * q[2], 0.f);
+      sampleN[p] = nn;
+      const float fn = (float)n;
+      for (int k = 0; k < 3; k++) {
+        const float4 g = b.gbuf[3 * (size_t)s + k];
+        float* o = planes[k] + 3 * (size_t)p;
+        o[0] = rInf * (g.x * fn) + oInf * o[0];
+        o[1] = rInf * (g.y * fn) + oInf * o[1];
+        o[2] = rInf * (g.z * fn) + oInf * o[2];
+      }
+    }
+    start += len;
+    if (!grid_barrier(coop, G, b.ctr)) return;
+  }
 }
 
 __global__ void k_fmath(int which, const float* x, uint32_t n, float* out) {
@@ -409,8 +643,51 @@ cudaError_t launch_adapt_budget(const FrameArgs& a, const RenderBuffers& b, cons
 cudaError_t launch_adapt_accum(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab, float* result,
                                uint32_t* sampleN, float* gpos, float* gnorm, float* gdiff, cudaStream_t st) {
   const uint32_t np = a.width * a.height;
-  k_accum<<<(np + 255) / 256, 256, 0, st>>>(a, b, ab.off, ab.cnt, result, sampleN, gpos, gnorm, gdiff);
+  k_accum<<<(uint32_t)(((size_t)np * 32 + 255) / 256), 256, 0, st>>>(a, b, ab.off, ab.cnt, result, sampleN, gpos,
+                                                                     gnorm, gdiff);
   return cudaGetLastError();
+}
+
+static uint32_t coop_grid(const void* kernel) {
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 256, 0);
+  if (per < 1) per = 1;
+  uint32_t g = (uint32_t)(sm_count() * per);
+  return g > kCoopPass - kCoopBlocks ? kCoopPass - kCoopBlocks : g;
+}
+
+cudaError_t launch_binary_budget(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab,
+                                 const float* result, const uint32_t* sampleN, uint32_t desired, float minProb,
+                                 cudaStream_t st) {
+  const uint32_t np = a.width * a.height;
+  const uint32_t nr = adapt_reduce_blocks(np);
+  k_error<<<nr, kReduceBlock, 0, st>>>(ab.filtered, result, sampleN, np, desired, ab.err, ab.partial);
+  cudaError_t e = cudaMemsetAsync(ab.coop, 0, 16 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  static uint32_t g = coop_grid((const void*)k_bin_search);
+  FrameArgs aa = a;
+  RenderBuffers bb = b;
+  const float* errp = ab.err;
+  uint32_t npv = np, Dv = desired;
+  float mp = minProb;
+  uint32_t* coop = ab.coop;
+  void* args[] = {&aa, &bb, &errp, &npv, &Dv, &mp, &coop};
+  e = cudaLaunchCooperativeKernel((const void*)k_bin_search, dim3(g), dim3(256), args, 0, st);
+  if (e != cudaSuccess) return e;
+  k_gen_queue<<<(np + 255) / 256, 256, 0, st>>>(a, b, np);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_binary_apply(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab, float* result,
+                                uint32_t* sampleN, float* gpos, float* gnorm, float* gdiff, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(ab.coop, 0, 2 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  static uint32_t g = coop_grid((const void*)k_bin_apply);
+  FrameArgs aa = a;
+  RenderBuffers bb = b;
+  uint32_t* coop = ab.coop;
+  void* args[] = {&aa, &bb, &coop, &result, &sampleN, &gpos, &gnorm, &gdiff};
+  return cudaLaunchCooperativeKernel((const void*)k_bin_apply, dim3(g), dim3(256), args, 0, st);
 }
 
 cudaError_t launch_fmath(int which, const float* x, uint32_t n, float* out, cudaStream_t st) {

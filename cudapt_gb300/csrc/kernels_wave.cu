@@ -22,6 +22,8 @@
 // grid-stride loop over them, so the host never waits on a count.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include "launch.h"
 #include "shade.cuh"
 #include "trace.cuh"
@@ -274,7 +276,7 @@ __global__ void __launch_bounds__(1024) k_light(DevScene S, FrameArgs a, float4*
     size += total;
     __syncthreads();
   }
-  if (x == 0) ctr->cacheSize = size;
+  if (x == 0) ctr->cacheSize[a.cacheSel] = size;
 }
 
 // ---------------------------------------------------------------------------
@@ -286,6 +288,7 @@ __global__ void k_camera(FrameArgs a, RenderBuffers b) {
   if (p == 0) {
     b.ctr->wave[0] = np;
     b.ctr->paths = np;
+    b.ctr->fetchT = 0;
   }
   if (p >= np) return;
   const uint32_t x = p % a.width, y = p / a.width;
@@ -322,182 +325,331 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, uint32_t v
 }
 
 // ---------------------------------------------------------------------------
-// Closest-hit traversal of one wave.
+// One persistent kernel walks the BVH for the extension rays of bounce d
+// (closest hit) and the shadow rays of bounce d-1 (any hit): the two sets
+// are independent, so running them in one launch removes one kernel tail per
+// bounce.  A lane takes a new ray as soon as its ray is finished (refill when
+// at least kRefill lanes of the warp are idle), so warps stay full while rays
+// last; extension rays are handed out first (they are the longer walks).
+// Every ray still visits nodes exactly in TracePrimitive's order, so per-ray
+// results do not depend on this scheduling.  The any-hit walk stops at the
+// first hit closer than maxDist: that is exactly when the reference's
+// closest-hit walk with the same maxDist would report a hit.
 template <bool kCount>
-__global__ void __launch_bounds__(kBlock) k_trace(DevScene S, RenderBuffers b, int in) {
-  const uint32_t n = b.ctr->wave[in];
+__global__ void __launch_bounds__(kBlock) k_walk(DevScene S, RenderBuffers b, int in, int shIn, int shReset,
+                                                 uint32_t kRefill) {
+  const uint32_t nE = (in >= 0) ? b.ctr->wave[in] : 0u;
+  const uint32_t nS = (shIn >= 0) ? b.ctr->shadow[shIn] : 0u;
+  const uint32_t n = nE + nS;
+  uint32_t* fetch = &b.ctr->fetchT;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    b.ctr->wave[in ^ 1] = 0;
-    b.ctr->shadow = 0;
+    atomicAdd(&b.ctr->rays, (unsigned long long)nS);
+    atomicAdd(&b.ctr->shadowRays, (unsigned long long)nS);
+    if (in >= 0) b.ctr->wave[in ^ 1] = 0;
+    b.ctr->shadow[shReset] = 0;
   }
-  const Wave w = b.wave[in];
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    const uint32_t i = base + threadIdx.x;
-    uint32_t nn = 0, nt = 0;
-    if (i < n) {
-      float4 o = w.o[i], d = w.d[i];
-      TraceHit h;
-      float4 r = make_float4(-1.f, 0.f, 0.f, 0.f);
-      if (trace_ref<false, kCount>(S, ld3(o), ld3(d), gb::kInf, gb::kBias, false, h, nn, nt))
-        r = make_float4(h.t, __uint_as_float(h.tri), h.u, h.v);
-      b.hit[i] = r;
-    }
-    if (kCount) {
-      warp_add_u64(&b.ctr->nodes, nn);
-      warp_add_u64(&b.ctr->tris, nt);
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Shading of one wave (pt_traceSample_kernel after TracePrimitive) and the
-// connection set-up of GetLightFromRandLightVertices / pt_connectEyeLightPath_kernel.
-__global__ void __launch_bounds__(kBlock) k_shade(DevScene S, FrameArgs a, RenderBuffers b, int in, uint32_t depth) {
-  using namespace gb;
-  const uint32_t n = b.ctr->wave[in];
-  const uint32_t cacheSize = b.ctr->cacheSize;
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.ctr->rays, (unsigned long long)n);
-  const Wave w = b.wave[in];
-  const Wave wo = b.wave[in ^ 1];
-  const uint32_t stride = gridDim.x * blockDim.x;
+  const Wave wv = b.wave[in >= 0 ? in : 0];
+  const float4* __restrict__ sh = b.sh[shIn >= 0 ? shIn : 0];
   const uint32_t lane = threadIdx.x & 31;
-  const f3 env = mk(a.env[0], a.env[1], a.env[2]);
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    const uint32_t i = base + threadIdx.x;
-    bool cont = false, conn = false;
-    float4 outO, outD, outT, outS, shA, shB, shC;
-    if (i < n) {
-      const float4 o4 = w.o[i], d4 = w.d[i], t4 = w.thr[i], s4 = w.smp[i], h4 = b.hit[i];
-      const uint32_t slot = __float_as_uint(o4.w);
-      const uint32_t pix = __float_as_uint(d4.w);
-      f3 orig = ld3(o4), dir = ld3(d4), outMul = ld3(t4), pathSample = ld3(s4);
-      if (h4.x < 0.f) {  // miss (:537-542), plus the optional environment term
-        if (a.useEnv) pathSample = pathSample + vmul(env, outMul);
-        float4 r = b.res[slot];
-        r = make_float4(r.x + pathSample.x, r.y + pathSample.y, r.z + pathSample.z,
-                        __uint_as_float(__float_as_uint(r.w) + 1u));
-        b.res[slot] = r;
-      } else {
-        const uint32_t smp = b.slotSmp[slot];
-        float u[8];
-        draw8(a.key0, a.key1, pix, a.frame, kEyeBounce, depth, smp, u);
-        const float hu = h4.z, hv = h4.w, hw = 1.f - hu - hv;
-        Surf sf = load_surf(S, __float_as_uint(h4.y), hw, hu, hv, a.gbuffer && depth == 0);
-        Mat m = load_mat(S, sf.mat);
-        Bounce B;
-        sample_bounce(orig, dir, h4.x, sf.norm, m, u, a.specPush != 0, B);
-        pathSample = pathSample + vmul(m.emis, outMul);
-        if (a.gbuffer && depth == 0) {  // AdapBilatAtomic.cu:471-476
-          b.gbuf[3 * (size_t)slot] = st4(sf.pos, 0.f);
-          b.gbuf[3 * (size_t)slot + 1] = st4(B.nl, 0.f);
-          b.gbuf[3 * (size_t)slot + 2] = st4(m.diff, 0.f);
-        }
-        const f3 inMul = outMul;
-        float contrib = length(outMul) * length(B.lmt);
-        if (length(m.emis) > 0.f) contrib = 0.f;
-        if (u[6] > contrib || depth + 1 >= a.eyeDepth) {
-          float4 r = b.res[slot];
-          r = make_float4(r.x + pathSample.x, r.y + pathSample.y, r.z + pathSample.z,
-                          __uint_as_float(__float_as_uint(r.w) + 1u));
-          b.res[slot] = r;
-        } else {
-          cont = true;
-          outMul = vmul(outMul, B.lmt);
-          outO = st4u(B.nOrig, slot);
-          outD = st4u(B.nDir, pix);
-          outT = st4(outMul, 0.f);
-          outS = st4(pathSample, 0.f);
-          if (B.type == kTypeDiff && cacheSize > 0) {
-            // connection (:665-723): everything but the visibility test
-            f3 pos = B.nOrig + B.nl * kBias;
-            uint32_t li = (uint32_t)(u[7] * (float)cacheSize);
-            if (li >= cacheSize) li = cacheSize - 1;
-            LV lv = load_lv(b.cache + 6 * (size_t)li);
-            f3 toDir = normalize(lv.pos - pos);
-            float toDist = length(lv.pos - pos);
-            if (length(lv.irrad) > 0.f && dot(B.nl, toDir) > 0.f) {
-              f3 irrad, irradDir;
-              if (toDist > kFltEps) {
-                irrad = shading(-1.f * toDir, lv.irradDir, lv.irrad, lv.norm, lv.diff, lv.metal, lv.rough, lv.spec,
-                                1.f, 1.f) +
-                        lv.emis;
-                irradDir = toDir;
-              } else {
-                irrad = lv.irrad;
-                irradDir = -1.f * lv.irradDir;
-              }
-              f3 c = vmax0(shading(-1.f * dir, irradDir, irrad, B.nl, m.diff, m.metal, m.rough, m.spec,
-                                   1.f - m.trans, 1.f));
-              if (length(c) > 0.f) {
-                conn = true;
-                shA = st4u(pos, slot);
-                shB = st4(toDir, toDist - kBias);
-                shC = st4(vmul(c, inMul), 0.f);
-              }
-            }
+  Walk w;
+  uint32_t stack[32];
+  bool has = false, drained = false, any = false;
+  uint32_t item = 0, nnE = 0, ntE = 0, nnS = 0, ntS = 0;
+  for (;;) {
+    const uint32_t idle = __ballot_sync(0xffffffffu, !has);
+    if (idle == 0xffffffffu && drained) break;
+    if (!drained && (idle == 0xffffffffu || __popc(idle) >= kRefill)) {
+      const uint32_t cnt = __popc(idle);
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(fetch, cnt);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + cnt >= n) drained = true;
+      if (!has) {
+        const uint32_t k = base + __popc(idle & lanemask_lt());
+        if (k < n) {
+          has = true;
+          any = k >= nE;
+          item = any ? k - nE : k;
+          if (any) {
+            const float4 A = sh[3 * (size_t)item], B = sh[3 * (size_t)item + 1];
+            w.init(ld3(A), ld3(B), B.w, gb::kBias, stack);
+          } else {
+            w.init(ld3(wv.o[item]), ld3(wv.d[item]), gb::kInf, gb::kBias, stack);
           }
         }
       }
     }
-    // append survivors / connection requests: one atomic per warp
-    const uint32_t mc = __ballot_sync(0xffffffffu, cont);
+    if (has && (any ? w.step<kCount>(S, stack, true, nnS, ntS) : w.step<kCount>(S, stack, false, nnE, ntE))) {
+      has = false;
+      if (any) {
+        if (!w.hit()) {  // unoccluded: the connection counts (:716-721)
+          const float4 A = sh[3 * (size_t)item], C = sh[3 * (size_t)item + 2];
+          const uint32_t slot = __float_as_uint(A.w);
+          const float4 r = b.res[slot];
+          b.res[slot] =
+              make_float4(r.x + C.x, r.y + C.y, r.z + C.z, __uint_as_float(__float_as_uint(r.w) + 4u));
+        }
+      } else {
+        b.hit[item] = w.hit() ? make_float4(w.minT, __uint_as_float(w.best), w.bu, w.bv)
+                              : make_float4(-1.f, 0.f, 0.f, 0.f);
+      }
+    }
+  }
+  if (kCount) {
+    warp_add_u64(&b.ctr->nodes, nnE);
+    warp_add_u64(&b.ctr->tris, ntE);
+    warp_add_u64(&b.ctr->nodesS, nnS);
+    warp_add_u64(&b.ctr->trisS, ntS);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Shading of one path after its closest-hit walk (pt_traceSample_kernel after
+// TracePrimitive, src/cudaRTBDPTStream.cu:381-543) and the connection set-up
+// of GetLightFromRandLightVertices / pt_connectEyeLightPath_kernel
+// (:665-723): everything but the visibility test, which the shadow walk does.
+// io holds the path (origin+slot, direction+pixel, throughput, carried
+// emission) on entry and the next ray's state on exit when cont is set.
+struct PathIO {
+  float4 o, d, t, s;
+  bool cont, conn;
+  float4 shA, shB, shC;
+};
+
+__device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a, const RenderBuffers& b,
+                                           const float4* __restrict__ cache, uint32_t cacheSize, uint32_t depth,
+                                           float4 h4, PathIO& io) {
+  using namespace gb;
+  io.cont = false;
+  io.conn = false;
+  const uint32_t slot = __float_as_uint(io.o.w);
+  const uint32_t pix = __float_as_uint(io.d.w);
+  f3 orig = ld3(io.o), dir = ld3(io.d), outMul = ld3(io.t), pathSample = ld3(io.s);
+  if (h4.x < 0.f) {  // miss (:537-542), plus the optional environment term
+    if (a.useEnv) pathSample = pathSample + vmul(mk(a.env[0], a.env[1], a.env[2]), outMul);
+    const float4 r = b.res[slot];
+    b.res[slot] = make_float4(r.x + pathSample.x, r.y + pathSample.y, r.z + pathSample.z,
+                              __uint_as_float(__float_as_uint(r.w) + 1u));
+    return;
+  }
+  const uint32_t smp = b.slotSmp[slot];
+  float u[8];
+  draw8(a.key0, a.key1, pix, a.frame, kEyeBounce, depth, smp, u);
+  const float hu = h4.z, hv = h4.w, hw = 1.f - hu - hv;
+  Surf sf = load_surf(S, __float_as_uint(h4.y), hw, hu, hv, a.gbuffer && depth == 0);
+  Mat m = load_mat(S, sf.mat);
+  Bounce B;
+  sample_bounce(orig, dir, h4.x, sf.norm, m, u, a.specPush != 0, B);
+  pathSample = pathSample + vmul(m.emis, outMul);
+  if (a.gbuffer && depth == 0) {  // AdapBilatAtomic.cu:471-476
+    b.gbuf[3 * (size_t)slot] = st4(sf.pos, 0.f);
+    b.gbuf[3 * (size_t)slot + 1] = st4(B.nl, 0.f);
+    b.gbuf[3 * (size_t)slot + 2] = st4(m.diff, 0.f);
+  }
+  const f3 inMul = outMul;
+  float contrib = length(outMul) * length(B.lmt);
+  if (length(m.emis) > 0.f) contrib = 0.f;
+  if (u[6] > contrib || depth + 1 >= a.eyeDepth) {
+    const float4 r = b.res[slot];
+    b.res[slot] = make_float4(r.x + pathSample.x, r.y + pathSample.y, r.z + pathSample.z,
+                              __uint_as_float(__float_as_uint(r.w) + 1u));
+    return;
+  }
+  io.cont = true;
+  outMul = vmul(outMul, B.lmt);
+  io.o = st4u(B.nOrig, slot);
+  io.d = st4u(B.nDir, pix);
+  io.t = st4(outMul, 0.f);
+  io.s = st4(pathSample, 0.f);
+  if (B.type != kTypeDiff || cacheSize == 0) return;
+  // connection: pick a cached light vertex, shade both ends (:665-723)
+  f3 pos = B.nOrig + B.nl * kBias;
+  uint32_t li = (uint32_t)(u[7] * (float)cacheSize);
+  if (li >= cacheSize) li = cacheSize - 1;
+  LV lv = load_lv(cache + 6 * (size_t)li);
+  f3 toDir = normalize(lv.pos - pos);
+  float toDist = length(lv.pos - pos);
+  if (!(length(lv.irrad) > 0.f && dot(B.nl, toDir) > 0.f)) return;
+  f3 irrad, irradDir;
+  if (toDist > kFltEps) {
+    irrad = shading(-1.f * toDir, lv.irradDir, lv.irrad, lv.norm, lv.diff, lv.metal, lv.rough, lv.spec, 1.f, 1.f) +
+            lv.emis;
+    irradDir = toDir;
+  } else {
+    irrad = lv.irrad;
+    irradDir = -1.f * lv.irradDir;
+  }
+  f3 c = vmax0(shading(-1.f * dir, irradDir, irrad, B.nl, m.diff, m.metal, m.rough, m.spec, 1.f - m.trans, 1.f));
+  if (length(c) > 0.f) {
+    io.conn = true;
+    io.shA = st4u(pos, slot);
+    io.shB = st4(toDir, toDist - kBias);
+    io.shC = st4(vmul(c, inMul), 0.f);
+  }
+}
+
+// Shading of one wave; survivors are appended to the other wave buffer and
+// connection requests to queue depth & 1, one atomic per warp each.
+// attach != 0 (the last bounce before the tail kernel): each continuing
+// path's connection record is stored at the path's own index j of queue
+// depth & 1 (slot word 0xffffffff when it has none), so that the tail kernel
+// walks it on the path's lane before the path's next bounce.
+__global__ void __launch_bounds__(kBlock) k_shade(DevScene S, FrameArgs a, RenderBuffers b, int in, uint32_t depth,
+                                                  uint32_t attach) {
+  const uint32_t n = b.ctr->wave[in];
+  const uint32_t cacheSize = b.ctr->cacheSize[a.cacheSel];
+  const float4* __restrict__ cache = b.cache[a.cacheSel];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(&b.ctr->rays, (unsigned long long)n);
+    b.ctr->fetchT = 0;  // for the next walk (next bounce's rays + this bounce's shadow rays)
+  }
+  const Wave w = b.wave[in];
+  const Wave wo = b.wave[in ^ 1];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t lane = threadIdx.x & 31;
+  float4* shq = b.sh[depth & 1u];
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    PathIO io;
+    io.cont = io.conn = false;
+    if (i < n) {
+      io.o = w.o[i];
+      io.d = w.d[i];
+      io.t = w.thr[i];
+      io.s = w.smp[i];
+      shade_path(S, a, b, cache, cacheSize, depth, b.hit[i], io);
+    }
+    const uint32_t mc = __ballot_sync(0xffffffffu, io.cont);
     if (mc) {
       uint32_t basej = 0;
       if (lane == 0) basej = atomicAdd(&b.ctr->wave[in ^ 1], __popc(mc));
       basej = __shfl_sync(0xffffffffu, basej, 0);
-      if (cont) {
-        uint32_t j = basej + __popc(mc & lanemask_lt());
-        wo.o[j] = outO;
-        wo.d[j] = outD;
-        wo.thr[j] = outT;
-        wo.smp[j] = outS;
+      if (io.cont) {
+        const uint32_t j = basej + __popc(mc & lanemask_lt());
+        wo.o[j] = io.o;
+        wo.d[j] = io.d;
+        wo.thr[j] = io.t;
+        wo.smp[j] = io.s;
+        if (attach) {
+          shq[3 * (size_t)j] = io.conn ? io.shA : make_float4(0.f, 0.f, 0.f, __uint_as_float(0xffffffffu));
+          shq[3 * (size_t)j + 1] = io.shB;
+          shq[3 * (size_t)j + 2] = io.shC;
+        }
       }
     }
-    const uint32_t ms = __ballot_sync(0xffffffffu, conn);
+    if (attach) continue;
+    const uint32_t ms = __ballot_sync(0xffffffffu, io.conn);
     if (ms) {
       uint32_t basej = 0;
-      if (lane == 0) basej = atomicAdd(&b.ctr->shadow, __popc(ms));
+      if (lane == 0) basej = atomicAdd(&b.ctr->shadow[depth & 1u], __popc(ms));
       basej = __shfl_sync(0xffffffffu, basej, 0);
-      if (conn) {
-        uint32_t j = basej + __popc(ms & lanemask_lt());
-        b.sh[3 * (size_t)j] = shA;
-        b.sh[3 * (size_t)j + 1] = shB;
-        b.sh[3 * (size_t)j + 2] = shC;
+      if (io.conn) {
+        const uint32_t j = basej + __popc(ms & lanemask_lt());
+        shq[3 * (size_t)j] = io.shA;
+        shq[3 * (size_t)j + 1] = io.shB;
+        shq[3 * (size_t)j + 2] = io.shC;
       }
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// Shadow rays: any-hit walk (same visiting order; stops at the first hit
-// closer than maxDist, which is exactly when the closest-hit walk would
-// report a hit); unoccluded connections add to their path (:716-721).
+// Tail of a frame: once few paths are left, per-bounce launches are bounded
+// by their slowest ray.  This persistent kernel instead carries every path
+// of wave `in` (at bounce depth0) through all its remaining bounces on one
+// lane: the connection attached to it by the previous bounce (queue shIn,
+// same index; slot word 0xffffffff: none), then closest-hit walk, shading,
+// connection and shadow walk bounce after bounce.  A path executes exactly
+// the operations of the wavefront kernels in the same order (a connection is
+// applied before the next bounce is shaded), so results are identical.
+enum : uint32_t { kIdle = 0, kPathExt = 1, kPathShadow = 2 };
+
 template <bool kCount>
-__global__ void __launch_bounds__(kBlock) k_shadow(DevScene S, RenderBuffers b) {
-  const uint32_t n = b.ctr->shadow;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    atomicAdd(&b.ctr->rays, (unsigned long long)n);
-    atomicAdd(&b.ctr->shadowRays, (unsigned long long)n);
-  }
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    const uint32_t j = base + threadIdx.x;
-    uint32_t nn = 0, nt = 0;
-    if (j < n) {
-      float4 A = b.sh[3 * (size_t)j], B = b.sh[3 * (size_t)j + 1];
-      TraceHit h;
-      if (!trace_ref<true, kCount>(S, ld3(A), ld3(B), B.w, gb::kBias, false, h, nn, nt)) {
-        float4 C = b.sh[3 * (size_t)j + 2];
-        const uint32_t slot = __float_as_uint(A.w);
-        float4 r = b.res[slot];
-        b.res[slot] = make_float4(r.x + C.x, r.y + C.y, r.z + C.z, __uint_as_float(__float_as_uint(r.w) + 4u));
+__global__ void __launch_bounds__(kBlock) k_tail(DevScene S, FrameArgs a, RenderBuffers b, int in, int shIn,
+                                                 uint32_t depth0, uint32_t kRefill) {
+  const uint32_t n = b.ctr->wave[in];
+  const uint32_t cacheSize = b.ctr->cacheSize[a.cacheSel];
+  const float4* __restrict__ cache = b.cache[a.cacheSel];
+  const float4* __restrict__ sh = b.sh[shIn >= 0 ? shIn : 0];
+  const Wave wv = b.wave[in];
+  const uint32_t lane = threadIdx.x & 31;
+  Walk w;
+  uint32_t stack[32];
+  PathIO io;
+  uint32_t mode = kIdle, depth = 0;
+  bool drained = false;
+  uint32_t extRays = 0, shRays = 0, nnE = 0, ntE = 0, nnS = 0, ntS = 0;
+  for (;;) {
+    const uint32_t idle = __ballot_sync(0xffffffffu, mode == kIdle);
+    if (idle == 0xffffffffu && drained) break;
+    if (!drained && (idle == 0xffffffffu || __popc(idle) >= kRefill)) {
+      const uint32_t cnt = __popc(idle);
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(&b.ctr->fetchT, cnt);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + cnt >= n) drained = true;
+      if (mode == kIdle) {
+        const uint32_t j = base + __popc(idle & lanemask_lt());
+        if (j < n) {
+          io.o = wv.o[j];
+          io.d = wv.d[j];
+          io.t = wv.thr[j];
+          io.s = wv.smp[j];
+          depth = depth0;
+          const float4 A = (shIn >= 0) ? sh[3 * (size_t)j] : make_float4(0.f, 0.f, 0.f, __uint_as_float(0xffffffffu));
+          if (__float_as_uint(A.w) != 0xffffffffu) {
+            io.shA = A;
+            io.shB = sh[3 * (size_t)j + 1];
+            io.shC = sh[3 * (size_t)j + 2];
+            mode = kPathShadow;
+            w.init(ld3(io.shA), ld3(io.shB), io.shB.w, gb::kBias, stack);
+          } else {
+            mode = kPathExt;
+            w.init(ld3(io.o), ld3(io.d), gb::kInf, gb::kBias, stack);
+          }
+        }
       }
     }
-    if (kCount) {
-      warp_add_u64(&b.ctr->nodesS, nn);
-      warp_add_u64(&b.ctr->trisS, nt);
+    if (mode == kIdle) continue;
+    const bool anyHit = mode == kPathShadow;
+    const bool done = anyHit ? w.step<kCount>(S, stack, true, nnS, ntS) : w.step<kCount>(S, stack, false, nnE, ntE);
+    if (!done) continue;
+    if (anyHit) {
+      shRays++;
+      if (!w.hit()) {  // unoccluded connection (:716-721)
+        const uint32_t slot = __float_as_uint(io.shA.w);
+        const float4 r = b.res[slot];
+        b.res[slot] = make_float4(r.x + io.shC.x, r.y + io.shC.y, r.z + io.shC.z,
+                                  __uint_as_float(__float_as_uint(r.w) + 4u));
+      }
+      mode = kPathExt;  // the path's next extension ray
+      w.init(ld3(io.o), ld3(io.d), gb::kInf, gb::kBias, stack);
+      continue;
     }
+    // closest hit of the path's current ray: shade it
+    extRays++;
+    const float4 h4 = w.hit() ? make_float4(w.minT, __uint_as_float(w.best), w.bu, w.bv)
+                              : make_float4(-1.f, 0.f, 0.f, 0.f);
+    shade_path(S, a, b, cache, cacheSize, depth, h4, io);
+    if (!io.cont) {
+      mode = kIdle;
+    } else {
+      depth++;
+      if (io.conn) {
+        mode = kPathShadow;
+        w.init(ld3(io.shA), ld3(io.shB), io.shB.w, gb::kBias, stack);
+      } else {
+        w.init(ld3(io.o), ld3(io.d), gb::kInf, gb::kBias, stack);
+      }
+    }
+  }
+  warp_add_u64(&b.ctr->rays, extRays + shRays);
+  warp_add_u64(&b.ctr->shadowRays, shRays);
+  if (kCount) {
+    warp_add_u64(&b.ctr->nodes, nnE);
+    warp_add_u64(&b.ctr->tris, ntE);
+    warp_add_u64(&b.ctr->nodesS, nnS);
+    warp_add_u64(&b.ctr->trisS, ntS);
   }
 }
 
@@ -564,6 +716,18 @@ __global__ void k_trace_rays(DevScene S, const float* rays, uint32_t n, float ma
 
 int g_sm = 0;
 
+// Idle lanes of a warp that trigger a refill in k_walk / k_tail (tuning
+// knob, GBPT_WALK_REFILL, 1..32; 24 by default: refilling only when most
+// lanes are idle keeps lanes that started together on nearby rays).
+uint32_t walk_refill() {
+  static uint32_t v = [] {
+    const char* e = std::getenv("GBPT_WALK_REFILL");
+    int x = e ? std::atoi(e) : 24;
+    return (uint32_t)(x < 1 ? 1 : x > 32 ? 32 : x);
+  }();
+  return v;
+}
+
 uint32_t grid_for(const void* kernel) {
   int per = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kBlock, 0);
@@ -586,7 +750,7 @@ int sm_count() {
 cudaError_t launch_light_pass(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, cudaStream_t st) {
   uint32_t threads = ((a.lightPaths + 31) / 32) * 32;
   if (threads == 0) threads = 32;
-  k_light<<<1, threads, 0, st>>>(S, a, b.cache, b.cacheCap, b.ctr);
+  k_light<<<1, threads, 0, st>>>(S, a, b.cache[a.cacheSel], b.cacheCap, b.ctr);
   return cudaGetLastError();
 }
 
@@ -596,32 +760,47 @@ cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream
   return cudaGetLastError();
 }
 
-cudaError_t launch_trace(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, cudaStream_t st) {
+cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
+                        int shReset, cudaStream_t st) {
   if (a.counting) {
-    static uint32_t g = grid_for((const void*)k_trace<true>);
-    k_trace<true><<<g, kBlock, 0, st>>>(S, b, in);
+    static uint32_t g = grid_for((const void*)k_walk<true>);
+    k_walk<true><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, walk_refill());
   } else {
-    static uint32_t g = grid_for((const void*)k_trace<false>);
-    k_trace<false><<<g, kBlock, 0, st>>>(S, b, in);
+    static uint32_t g = grid_for((const void*)k_walk<false>);
+    k_walk<false><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, walk_refill());
   }
   return cudaGetLastError();
+}
+
+cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
+                        uint32_t depth0, cudaStream_t st) {
+  if (a.counting) {
+    static uint32_t g = grid_for((const void*)k_tail<true>);
+    k_tail<true><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill());
+  } else {
+    static uint32_t g = grid_for((const void*)k_tail<false>);
+    k_tail<false><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill());
+  }
+  return cudaGetLastError();
+}
+
+uint32_t tail_from(uint32_t eyeDepth) {
+  // default: the last 4 bounces (measured on the 1024x768 interior, depth 10:
+  // tail kernel from bounce 6 beats both per-bounce launches throughout and
+  // earlier switches; the tail kernel's 107 registers cost occupancy while
+  // many paths are alive)
+  static int v = [] {
+    const char* e = std::getenv("GBPT_TAIL_FROM");
+    return e ? std::atoi(e) : -2;
+  }();
+  if (v == -2) return eyeDepth > 6 ? eyeDepth - 4 : eyeDepth;
+  return v < 0 ? eyeDepth : (uint32_t)v;
 }
 
 cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t depth,
-                         cudaStream_t st) {
+                         bool attach, cudaStream_t st) {
   static uint32_t g = grid_for((const void*)k_shade);
-  k_shade<<<g, kBlock, 0, st>>>(S, a, b, in, depth);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_shadow(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, cudaStream_t st) {
-  if (a.counting) {
-    static uint32_t g = grid_for((const void*)k_shadow<true>);
-    k_shadow<true><<<g, kBlock, 0, st>>>(S, b);
-  } else {
-    static uint32_t g = grid_for((const void*)k_shadow<false>);
-    k_shadow<false><<<g, kBlock, 0, st>>>(S, b);
-  }
+  k_shade<<<g, kBlock, 0, st>>>(S, a, b, in, depth, attach ? 1u : 0u);
   return cudaGetLastError();
 }
 

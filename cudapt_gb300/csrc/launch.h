@@ -27,11 +27,12 @@ struct DevScene {
 // Counters shared by the kernels of one renderer (device memory).
 struct DevCounters {
   uint32_t wave[2];       // paths in the two ping-pong wave buffers
-  uint32_t shadow;        // connection (shadow) rays queued this bounce
-  uint32_t cacheSize;     // light-vertex cache entries
+  uint32_t shadow[2];     // connection (shadow) rays queued by bounce d in queue d & 1
+  uint32_t cacheSize[2];  // entries of the two light-vertex caches
   uint32_t paths;         // camera paths of the current frame
   uint32_t errFlags;      // bit 0: light cache overflow, bit 1: bounds
-  uint32_t pad[2];
+  uint32_t fetchT;        // next ray handed to a lane by the persistent walk kernel
+  uint32_t fetchS;        // unused (kept for layout)
   unsigned long long rays, nodes, tris;  // cumulative work counters (closest-hit walks)
   unsigned long long shadowRays, nodesS, trisS;  // any-hit (shadow) walks
   double errSum;          // adaptive: sum of per-pixel errors
@@ -56,17 +57,20 @@ struct FrameArgs {
   uint32_t gbuffer;     // record first-hit position/normal/diffuse
   uint32_t counting;    // node/triangle counters
   uint32_t useEnv;      // env != 0: add env * throughput on a miss
+  uint32_t cacheSel;    // light-vertex cache (0/1) this frame reads or the light pass writes
 };
 
 struct RenderBuffers {
   Wave wave[2];
   float4* hit;          // t, tri bits, u, v (t < 0: miss)
-  float4* sh;           // 3 per entry: {origin, slot} {dir, maxDist} {weighted contribution}
+  float4* sh[2];        // connection queues (bounce parity), 3 float4 per entry:
+                        // {origin, slot} {dir, maxDist} {weighted contribution}
   float4* res;          // per slot: acc.xyz, n bits
   float4* gbuf;         // per slot: 3 float4 (pos, normal, diffuse) when gbuffer
   uint32_t* slotPix;    // per slot pixel id
   uint32_t* slotSmp;    // per slot sample id
-  float4* cache;        // light vertices, 6 float4 each
+  float4* cache[2];     // two light-vertex caches (6 float4 per vertex): one is read by the
+                        // current frames while the next light pass fills the other
   DevCounters* ctr;
   uint32_t cap;         // slots
   uint32_t cacheCap;    // light vertices
@@ -75,10 +79,20 @@ struct RenderBuffers {
 // wavefront kernels (kernels_wave.cu)
 cudaError_t launch_light_pass(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, cudaStream_t st);
 cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream_t st);
-cudaError_t launch_trace(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, cudaStream_t st);
+// one persistent walk over the extension rays of wave `in` (in < 0: none)
+// followed by the shadow rays of connection queue `shIn` (shIn < 0: none);
+// resets the counters of wave in^1 and of connection queue `shReset`
+cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
+                        int shReset, cudaStream_t st);
+// attach: store each continuing path's connection at the path's index (for the tail kernel)
 cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t depth,
-                         cudaStream_t st);
-cudaError_t launch_shadow(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, cudaStream_t st);
+                         bool attach, cudaStream_t st);
+// remaining bounces of every path of wave `in` (at bounce depth0), starting
+// with the connection attached to it in queue shIn; one lane per path
+cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
+                        uint32_t depth0, cudaStream_t st);
+// first bounce handled by the tail kernel (GBPT_TAIL_FROM, < 0: never; default D-4 for D > 6)
+uint32_t tail_from(uint32_t eyeDepth);
 cudaError_t launch_apply(const FrameArgs& a, const RenderBuffers& b, float* result, uint32_t* sampleN, float* gpos,
                          float* gnorm, float* gdiff, cudaStream_t st);
 cudaError_t launch_trace_rays(const DevScene& S, const float* rays, uint32_t n, float maxDist, float eps, int cullback,
@@ -93,7 +107,9 @@ struct AdaptBuffers {
   uint32_t* blockSum;  // per scan block
   double* partial;     // per reduce block
   float* filtered;     // W*H*3
+  uint32_t* coop;      // binary allocator: barrier words, per-block counts, pass table
 };
+constexpr uint32_t kCoopWords = 8192;  // coop buffer size (uint32 words)
 cudaError_t launch_bilateral(const float* color, const float* pos, const float* norm, const float* emit, uint32_t W,
                              uint32_t H, float ceud, float peud, float neud, float eeud, uint32_t radius,
                              const float* g, float* out, cudaStream_t st);
@@ -101,6 +117,14 @@ cudaError_t launch_adapt_budget(const FrameArgs& a, const RenderBuffers& b, cons
                                 const float* result, const uint32_t* sampleN, uint32_t desired, cudaStream_t st);
 cudaError_t launch_adapt_accum(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab, float* result,
                                uint32_t* sampleN, float* gpos, float* gnorm, float* gdiff, cudaStream_t st);
+// binary allocator (src/cudaRTBDPTStreamAdapBilatBinary.cu:1316-1418):
+// error, cooperative window search + queue, camera paths for the queue
+cudaError_t launch_binary_budget(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab,
+                                 const float* result, const uint32_t* sampleN, uint32_t desired, float minProb,
+                                 cudaStream_t st);
+// running means of the queue, pass by pass (pt_applyPathQueueResult_kernel per pass)
+cudaError_t launch_binary_apply(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab, float* result,
+                                uint32_t* sampleN, float* gpos, float* gnorm, float* gdiff, cudaStream_t st);
 uint32_t adapt_scan_blocks(uint32_t np);
 uint32_t adapt_reduce_blocks(uint32_t np);
 cudaError_t launch_fmath(int which, const float* x, uint32_t n, float* out, cudaStream_t st);

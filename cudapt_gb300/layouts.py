@@ -55,6 +55,7 @@ PARAMS = np.dtype(
         ("filter_diffuse", "<u4"),
         ("filter_sigma_spatial", "<f4"),
         ("request_id", "<u4"),
+        ("min_trace_prob", "<f4"),
     ]
 )
 
@@ -62,6 +63,7 @@ PARAMS = np.dtype(
 # include/raytracer.h:13-23).
 MODE_BDPT_SC = 0              # "BDPTSC"                     cudaRTBDPTStream
 MODE_BDPT_SC_ADAP_BILAT = 1   # "BDPTSC Adap Bilat PLL"      cudaRTBDPTStreamAdapBilatAtomic
+MODE_BDPT_SC_ADAP_BILAT_BINARY = 2  # "BDPTSC Adap Bilat Binary"  cudaRTBDPTStreamAdapBilatBinary
 
 
 def default_params(**over):
@@ -85,9 +87,23 @@ def default_params(**over):
     p["filter_diffuse"] = 0
     p["filter_sigma_spatial"] = 0.0
     p["request_id"] = 0
+    p["min_trace_prob"] = 0.0
     for k, v in over.items():
         p[k] = v
     return p
+
+
+def as_params(p):
+    """A PARAMS record from any record with a subset of its fields (older layouts
+    included); missing fields keep their defaults."""
+    out = default_params()
+    if p is None:
+        return out
+    p = np.asarray(p)
+    for name in p.dtype.names or ():
+        if name in PARAMS.names:
+            out[name] = p[name]
+    return out
 
 
 def material(diffuse=(1.0, 1.0, 1.0), emissive=(0.0, 0.0, 0.0), specular=0.5, metallic=0.0,

@@ -81,13 +81,15 @@ typedef struct gbpt_params {
   float filter_sigma_spatial; /* spatial Gaussian sigma in pixels; <= 0 keeps the
                                  reference's table built from the colour delta */
   uint32_t request_id;      /* Philox key word 1 (0) */
+  float min_trace_prob;     /* "Min Trace Probability" of the binary allocator (0) */
 } gbpt_params;
 
 /* Renderer modes: the BDPT entries of the X-macro registry
  * (include/raytracer.h:13-23). */
 typedef enum gbpt_mode {
-  GBPT_MODE_BDPT_SC = 0,            /* "BDPTSC"                 cudaRTBDPTStream */
-  GBPT_MODE_BDPT_SC_ADAP_BILAT = 1  /* "BDPTSC Adap Bilat PLL"  cudaRTBDPTStreamAdapBilatAtomic */
+  GBPT_MODE_BDPT_SC = 0,                  /* "BDPTSC"                    cudaRTBDPTStream */
+  GBPT_MODE_BDPT_SC_ADAP_BILAT = 1,       /* "BDPTSC Adap Bilat PLL"     cudaRTBDPTStreamAdapBilatAtomic */
+  GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY = 2 /* "BDPTSC Adap Bilat Binary"  cudaRTBDPTStreamAdapBilatBinary */
 } gbpt_mode;
 
 /* Per-frame statistics (the reference's PERFBREAKDOWN timers,
@@ -104,9 +106,9 @@ typedef struct gbpt_stats {
   uint64_t shadow_tris;    /* any-hit triangle tests (counting on) */
   float ms_total;          /* device time of the frame */
   float ms_light;          /* light pass */
-  float ms_trace;          /* closest-hit traversal kernels */
+  float ms_trace;          /* BVH walks: extension rays and, in the same launches, shadow rays */
   float ms_shade;          /* shading / compaction kernels */
-  float ms_shadow;         /* shadow-ray kernels */
+  float ms_shadow;         /* 0: shadow rays are walked together with the next bounce's rays */
   float ms_filter;         /* bilateral filter */
   float ms_adapt;          /* error, budget and accumulation kernels */
 } gbpt_stats;

@@ -143,8 +143,9 @@ class Renderer:
     """Oracle renderer: one call of render() adds `frames` progressive passes."""
 
     def __init__(self, width, height, mode, params, threads=None):
+        from cudapt_gb300.layouts import as_params
         self.W, self.H = width, height
-        self.params = np.array(params)
+        self.params = as_params(params)
         self.h = lib().orc_renderer_create(width, height, mode, _p(self.params), threads or os.cpu_count())
 
     def __del__(self):
@@ -189,9 +190,10 @@ class Renderer:
 
 
 def render_fp64(scene, params, width, height, cam, frames, threads=None):
+    from cudapt_gb300.layouts import as_params
     out = np.zeros(width * height * 3, np.float64)
     c = cam_array(cam)
-    p = np.array(params)
+    p = as_params(params)
     lib().orc_render_fp64(scene.h, _p(p), width, height, _p(c), frames, threads or os.cpu_count(), _p(out))
     return out
 

@@ -733,6 +733,7 @@ void default_params(Params* p) {
   p->filter_diffuse = 0;
   p->filter_sigma_spatial = 0.f;
   p->request_id = 0;
+  p->min_trace_prob = 0.f;
 }
 
 void renderer_init(Renderer* r, uint32_t W, uint32_t H, int32_t mode, const Params& p, bool fp64, uint32_t threads) {
@@ -848,7 +849,8 @@ void render_frame(Renderer* r, const Scene& s, const Camera& cam) {
   const uint32_t np = r->W * r->H;
   if (r->frame % r->p.light_every == 0) light_pass(r, s, r->frame);
 
-  const bool adaptive = r->mode == kModeAdaptive;
+  const bool adaptive = r->mode == kModeAdaptive || r->mode == kModeAdaptiveBinary;
+  const bool binary = r->mode == kModeAdaptiveBinary;
   const bool frame0 = r->frame == 0;
   std::vector<uint32_t> pixOf, sampleOf;
   bool uniform = !adaptive || r->frame < r->p.warmup_frames;
@@ -879,7 +881,47 @@ void render_frame(Renderer* r, const Scene& s, const Camera& cam) {
     float sumF = (float)sum;
     const uint32_t gen = np;
     uint64_t total = 0;
-    for (uint32_t i = 0; i < np; i++) {  // pt_genAdapPathQueue_kernel :817-842
+    if (binary) {
+      // binary search of an acceptance scale (AdapBilatBinary.cu:1316-1384):
+      // each pass accepts pixel p when u * mid <= max(e_p, minTraceProb),
+      // appends the accepted pixels in pixel order, and halves the window
+      // towards W*H/D accepted paths; leftover slots get pixel ids 0, 1, ...
+      float maxE = 0.f;
+      for (uint32_t i = 0; i < np; i++) maxE = (maxE < r->err[i]) ? r->err[i] : maxE;  // thrust::maximum
+      float left = 0.f, right = maxE * 2.f;
+      const float desired = (float)np / (float)D;
+      uint32_t accum = 0;
+      r->chunks.clear();
+      for (uint32_t pass = 0; accum < gen && pass < 64; pass++) {
+        const float mid = (left + right) * 0.5f;
+        uint32_t take = 0;
+        for (uint32_t i = 0; i < np && accum + take < gen; i++) {
+          U4 rr = philox4x32_10(U4{{i, r->frame, (uint32_t)kBinaryAccept << 24, pass}}, r->p.seed, r->p.request_id);
+          float th = std::fmax(r->err[i], r->p.min_trace_prob);
+          if (!(u01(rr.v[0]) * mid > th)) {
+            pixOf.push_back(i);
+            sampleOf.push_back(pass);
+            take++;
+          }
+        }
+        r->chunks.push_back(take);
+        accum += take;
+        if (take == 0) break;
+        if ((float)take < desired)
+          right = mid;
+        else if ((float)take > desired)
+          left = mid;
+      }
+      if (accum < gen) {
+        uint32_t fill = gen - accum;
+        for (uint32_t k = 0; k < fill; k++) {
+          pixOf.push_back(k);
+          sampleOf.push_back((uint32_t)r->chunks.size());
+        }
+        r->chunks.push_back(fill);
+      }
+    }
+    for (uint32_t i = 0; i < np && !binary; i++) {  // pt_genAdapPathQueue_kernel :817-842
       float ratio = r->err[i] / sumF;
       float v = (float)gen * ratio;
       uint32_t cnt = (v >= 1.f && v < 4294967040.f) ? (uint32_t)v : 0u;
@@ -894,7 +936,7 @@ void render_frame(Renderer* r, const Scene& s, const Camera& cam) {
   }
 
   std::vector<PathResult> res;
-  trace_pixels<float>(r, s, c, pixOf, sampleOf, res, adaptive);
+  trace_pixels<float>(r, s, c, pixOf, sampleOf, res, r->mode == kModeAdaptive);  // spec push: PLL variant only
   r->lastPaths = res.size();
   r->lastRays = r->lastNodes = r->lastTris = 0;
   for (auto& q : res) {
@@ -903,6 +945,13 @@ void render_frame(Renderer* r, const Scene& s, const Camera& cam) {
     r->lastTris += q.tris;
   }
   float* g3[3] = {r->gpos.data(), r->gnorm.data(), r->gdiff.data()};
+  if (!uniform && binary) {  // pt_applyPathQueueResult_kernel per pass, in pass order (:1396-1418)
+    for (size_t k = 0; k < pixOf.size(); k++) {
+      const double* gs[3] = {res[k].gpos, res[k].gnorm, res[k].gdiff};
+      apply_mean(r->result.data(), r->sampleN.data(), pixOf[k], res[k].acc, res[k].n, frame0, g3, gs);
+    }
+    return;
+  }
   if (uniform) {
     for (uint32_t i = 0; i < np; i++) {
       const double* gs[3] = {res[i].gpos, res[i].gnorm, res[i].gdiff};
@@ -910,24 +959,53 @@ void render_frame(Renderer* r, const Scene& s, const Camera& cam) {
     }
     return;
   }
-  // ordered per-pixel sums (pt_atomicApplyPathQueueResult_kernel :1041-1085,
-  // then pt_accumTempResultToResult_kernel :1088-1141)
+  // per-pixel sums (pt_atomicApplyPathQueueResult_kernel :1041-1085, then
+  // pt_accumTempResultToResult_kernel :1088-1141) in the library's fixed
+  // order: 32 lane partials (lane l adds samples l, l+32, ...), then a
+  // butterfly x[l] = x[l] + x[l^m] for m = 16, 8, 4, 2, 1.
   size_t q = 0;
   for (uint32_t i = 0; i < np; i++) {
-    float tr[3] = {0, 0, 0}, tp[3] = {0, 0, 0}, tn[3] = {0, 0, 0}, td[3] = {0, 0, 0};
-    uint32_t tN = 0;
-    for (uint32_t k = 0; k < r->counts[i]; k++, q++) {
-      const PathResult& pr = res[q];
+    float part[32][12];
+    uint32_t pn[32];
+    for (int l = 0; l < 32; l++) {
+      pn[l] = 0;
+      for (int k = 0; k < 12; k++) part[l][k] = 0.f;
+    }
+    for (uint32_t k = 0; k < r->counts[i]; k++) {
+      const PathResult& pr = res[q + k];
       float a[3] = {(float)pr.acc[0], (float)pr.acc[1], (float)pr.acc[2]};
       if (std::isinf(a[0]) || std::isinf(a[1]) || std::isinf(a[2])) continue;
+      float* v = part[k & 31];
+      float fn = (float)pr.n;
       for (int c3 = 0; c3 < 3; c3++) {
-        tr[c3] = tr[c3] + a[c3];
-        tp[c3] = tp[c3] + (float)pr.gpos[c3] * (float)pr.n;
-        tn[c3] = tn[c3] + (float)pr.gnorm[c3] * (float)pr.n;
-        td[c3] = td[c3] + (float)pr.gdiff[c3] * (float)pr.n;
+        v[c3] = v[c3] + a[c3];
+        v[3 + c3] = v[3 + c3] + (float)pr.gpos[c3] * fn;
+        v[6 + c3] = v[6 + c3] + (float)pr.gnorm[c3] * fn;
+        v[9 + c3] = v[9 + c3] + (float)pr.gdiff[c3] * fn;
       }
-      tN += pr.n;
+      pn[k & 31] += pr.n;
     }
+    q += r->counts[i];
+    for (int m = 16; m > 0; m >>= 1) {
+      float nxt[32][12];
+      uint32_t nn2[32];
+      for (int l = 0; l < 32; l++) {
+        for (int k = 0; k < 12; k++) nxt[l][k] = part[l][k] + part[l ^ m][k];
+        nn2[l] = pn[l] + pn[l ^ m];
+      }
+      for (int l = 0; l < 32; l++) {
+        pn[l] = nn2[l];
+        for (int k = 0; k < 12; k++) part[l][k] = nxt[l][k];
+      }
+    }
+    float tr[3], tp[3], tn[3], td[3];
+    for (int c3 = 0; c3 < 3; c3++) {
+      tr[c3] = part[0][c3];
+      tp[c3] = part[0][3 + c3];
+      tn[c3] = part[0][6 + c3];
+      td[c3] = part[0][9 + c3];
+    }
+    uint32_t tN = pn[0];
     uint32_t N = r->sampleN[i];
     if (frame0) {
       N = 0;

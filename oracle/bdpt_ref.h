@@ -28,9 +28,10 @@ struct Params {
   uint32_t filter_diffuse;   // "Filter Diffuse Flag" 0
   float filter_sigma_spatial;  // <= 0: the reference's quirk (spatial table from the colour delta)
   uint32_t request_id;       // Philox key word 1
+  float min_trace_prob;      // "Min Trace Probability" (AdapBilatBinary.cu:28), binary allocator
 };
 
-enum Mode : int32_t { kModeBDPT = 0, kModeAdaptive = 1 };
+enum Mode : int32_t { kModeBDPT = 0, kModeAdaptive = 1, kModeAdaptiveBinary = 2 };
 
 struct Camera {
   float pos[3], dir[3], up[3];
@@ -60,6 +61,7 @@ struct Renderer {
   float camBasis[9] = {0};  // pos, dir, up after orthonormalisation
   std::vector<float> result, gpos, gnorm, gdiff, filtered, err;
   std::vector<uint32_t> sampleN, counts;
+  std::vector<uint32_t> chunks;  // binary allocator: paths per pass (last = fill)
   std::vector<LightVertex> cache;
   uint32_t cacheSize = 0;
   uint32_t threads = 1;

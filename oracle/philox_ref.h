@@ -42,7 +42,7 @@ static inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
 static inline float u01(uint32_t x) { return (float)(x >> 9) * 0x1p-23f + 0x1p-24f; }
 
 // Counter layout shared with the CUDA kernels.
-enum Stream : uint32_t { kCamera = 0, kEyeBounce = 1, kLightGen = 2, kLightBounce = 3 };
+enum Stream : uint32_t { kCamera = 0, kEyeBounce = 1, kLightGen = 2, kLightBounce = 3, kBinaryAccept = 4 };
 
 static inline void draw8(uint32_t key0, uint32_t key1, uint32_t pathId, uint32_t frame, uint32_t stream, uint32_t depth,
                          uint32_t sample, float u[8]) {

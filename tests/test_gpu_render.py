@@ -117,6 +117,19 @@ def test_adaptive_matches(gbdev, orc):
     assert abs(img.mean() - want.mean()) <= 2e-3 * want.mean()
 
 
+def test_adaptive_binary_matches(gbdev, orc):
+    """'BDPTSC Adap Bilat Binary': window search passes, leftover fill, per-pass apply."""
+    r, ref, img, want, stats = _render_both(gbdev, orc, "cornell", 64, 48, 5, mode=2, eye_depth_max=8,
+                                            light_depth_max=8, warmup_frames=2, filter_radius=4)
+    same = np.mean(img.view(np.uint32) == want.view(np.uint32))
+    assert same >= 0.99, same
+    sn_gpu = r.read_buffer(6)
+    sn_ref, _ = ref.sample_counts()
+    assert np.mean(sn_gpu == sn_ref) >= 0.99
+    assert sn_gpu.sum() > 64 * 48 * 4  # the budgeted frames added W*H paths each
+    np.testing.assert_allclose(r.read_buffer(1), ref.get(1), rtol=1e-5, atol=1e-6)
+
+
 def test_bilateral_kernel_bitexact(gbdev, orc):
     rng = np.random.Generator(np.random.PCG64(21))
     W, H = 77, 45
@@ -151,3 +164,29 @@ def test_errors_are_reported(gbdev):
         gb.RTRenderer(16, 16, params=gb.default_params(light_paths=5000))
     with pytest.raises(gb.GbptError):
         r.attr_set("No Such Attribute", 1.0)
+
+
+def test_fp32_converges_to_fp64_reference(gbdev, orc):
+    """RMSE against the FP64 host render of the same estimator: the GPU's FP32
+    image after F frames is far closer to the FP64 image of the same F frames
+    (same random numbers) than two independent F-frame images are to each
+    other, and the error of independent runs shrinks as frames grow."""
+    (v, t, m), cam = scene_arrays("cornell")
+    W = H = 32
+    params = gbdev.default_params(eye_depth_max=8, light_depth_max=8)
+    s = gbdev.RTScene(v, t, m).build_bvh()
+    osc = orc.Scene(v, t, m)
+    ref64 = {}
+    for F in (8, 32):
+        r = gbdev.RTRenderer(W, H, 0, params)
+        for _ in range(F):
+            img = r.render(s, cam).astype(np.float64)
+        ref64[F] = orc.render_fp64(osc, params, W, H, cam, F)
+        rmse_same = np.sqrt(np.mean((img - ref64[F]) ** 2))
+        other = gbdev.RTRenderer(W, H, 0, gbdev.default_params(eye_depth_max=8, light_depth_max=8, seed=4321))
+        for _ in range(F):
+            img2 = other.render(s, cam).astype(np.float64)
+        rmse_indep = np.sqrt(np.mean((img2 - ref64[F]) ** 2))
+        assert rmse_same < 0.15 * rmse_indep, (F, rmse_same, rmse_indep)
+        ref64[F, "indep"] = rmse_indep
+    assert ref64[32, "indep"] < ref64[8, "indep"]

@@ -129,21 +129,26 @@ def params_for(gb_or_layouts, **kw):
 W, H = WL[1], WL[2]
 
 
-def run_cpu_sample(threads, rows, frames=1, seed=1234):
-    """Oracle (CPU restatement of the reference estimator) on a band of rows of
-    the same workload; returns (paths, seconds, build_seconds)."""
+def run_cpu_sample(threads, rows, frames=1, seed=1234, bands=4):
+    """Oracle (CPU restatement of the reference estimator) on `rows` full-width
+    rows of the same workload, split into `bands` bands spread evenly over the
+    image so that the sample's cost per path matches the whole frame's;
+    returns (paths, seconds, build_seconds)."""
     import oracle
     from cudapt_gb300 import layouts
     (v, t, m), cam = scene_and_camera()
     sc = oracle.Scene(v, t, m)
     p = params_for(layouts, seed=seed)
-    # a band of `rows` full-width rows: same pixels-per-path cost as the full frame
-    band_cam = dict(cam)
-    r = oracle.Renderer(W, rows, 0, p, threads=threads)
-    r.set_window(0, 0, W, H)
-    t0 = time.perf_counter()
-    r.render(sc, band_cam, frames)
-    dt = time.perf_counter() - t0
+    bands = max(1, min(bands, rows))
+    per = [rows // bands + (1 if b < rows % bands else 0) for b in range(bands)]
+    dt = 0.0
+    for b, rb in enumerate(per):
+        y0 = (H - rb) * b // max(bands - 1, 1)
+        r = oracle.Renderer(W, rb, 0, p, threads=threads)
+        r.set_window(0, y0, W, H)
+        t0 = time.perf_counter()
+        r.render(sc, cam, frames)
+        dt += time.perf_counter() - t0
     return W * rows * frames, dt, sc.build_seconds
 
 
@@ -152,8 +157,8 @@ def bench_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    # bounded sample per step: a 1024 x rows band; rows sized for ~10 s per step
-    rows = int(os.environ.get("GBPT_REF_ROWS", "48"))
+    # bounded sample per step: a quarter of the frame's rows in 4 bands
+    rows = int(os.environ.get("GBPT_REF_ROWS", str(H // 4)))
     for _ in range(args.warmup if args.warmup < 1 else 1):
         run_cpu_sample(threads, 4)
     paths = secs = 0.0
@@ -167,9 +172,9 @@ def bench_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "width": W, "height": H, "paths_per_step": W * rows,
-                   "sample": f"{W}x{rows} row band per step (full-width rows of the same frame)"},
+                   "sample": f"{W}x{rows} rows per step in 4 bands spread over the frame"},
         "cpu_baseline": {"value": round(v, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
-                         "sample": f"{W}x{rows} band x {args.steps} steps, oracle FP32 estimator + restated BVH build "
+                         "sample": f"{W}x{rows} rows (4 bands) x {args.steps} steps, oracle FP32 estimator + restated BVH build "
                                    f"({build_s:.2f} s build)"},
         "e2e": {"value": round(v, 4), "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -204,6 +209,7 @@ def bench_gpu(args):
               "ms_total": 0.0}
     rays = 0
     paths = 0
+    launches = 0
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
             flush()
@@ -211,6 +217,7 @@ def bench_gpu(args):
             ms.append(st["ms_total"])
             rays += st["rays"]
             paths += st["paths"]
+            launches += st["launches"]
             for k in phases:
                 phases[k] += st[k]
     total_ms = float(np.sum(ms))
@@ -236,18 +243,14 @@ def bench_gpu(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        rows = int(os.environ.get("GBPT_CPU_ROWS", "24"))
+        rows = int(os.environ.get("GBPT_CPU_ROWS", str(H)))  # the whole frame
         p, dt, bs = run_cpu_sample(threads, rows)
         cpu = {"value": round(p / dt / 1e6, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
-               "sample": f"{W}x{rows} row band of one uniform frame, oracle FP32 estimator "
+               "sample": f"{W}x{rows} rows (4 bands spread over the frame) of one uniform frame, oracle FP32 estimator "
                          f"({bs:.2f} s restated BVH build)"}
 
     D = int(params["eye_depth_max"])
-    # camera + D x (walk, shade) + final walk + apply; budgeted frames: filter +
-    # 6 budget kernels + D x (walk, shade) + final walk + accumulate
-    launches_per_frame = 2 * D + 3 if WL[3] == 0 else 2 * D + 9
-    light_frames = sum(1 for f in range(args.warmup, args.warmup + args.steps)
-                       if f % int(params["light_every"]) == 0)
+    traffic = profiled_traffic(args.workload)
     line = {
         "metric": METRIC, "value": round(value * world, 3), "unit": "Mpaths/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
@@ -261,17 +264,32 @@ def bench_gpu(args):
                    "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": round(e2e * world, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": 40,
                 "d2h_bytes_per_step": np_ * 12},
-        "roofline": {"bound": "hbm", "kernel": "k_walk (closest-hit + shadow BVH walks)",
+        "roofline": {"bound": "hbm", "kernel": "k_walk + k_tail (closest-hit + shadow BVH walks of one frame)",
                      "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4) if achieved else None, "peak_kind": peak_kind,
-                     "traffic": None,
+                     "traffic": traffic,
                      "algorithmic_bytes_per_frame": int(trace_bytes)},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
-        "gpu_launches": args.steps * launches_per_frame + light_frames,
+        "gpu_launches": launches,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def profiled_traffic(workload):
+    """DRAM bytes (read + write) of the BVH-walk launches of one frame, from the
+    committed ncu summary of this workload (profiles/walk_traffic_<workload>.txt,
+    line ``traffic_bytes_per_frame <n>``); None when no capture exists."""
+    p = os.path.join(ROOT, "profiles", f"walk_traffic_{workload}.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for ln in f:
+            parts = ln.split()
+            if len(parts) == 2 and parts[0] == "traffic_bytes_per_frame":
+                return int(parts[1])
+    return None
 
 
 class FlushBuffer:

@@ -11,12 +11,14 @@ import numpy as np
 
 from . import layouts
 from ._native import GbptError, Stats, as_c, check, load, ptr
-from .layouts import (MATERIAL, MODE_BDPT_SC, MODE_BDPT_SC_ADAP_BILAT, MODE_BDPT_SC_ADAP_BILAT_BINARY, PARAMS,
-                      TRIANGLE, VERTEX, default_params, material)
+from .layouts import (MATERIAL, MODE_BDPT_SC, MODE_BDPT_SC_ADAP_BILAT, MODE_BDPT_SC_ADAP_BILAT_BINARY,
+                      MODE_BDPT_SC_BILAT, MODE_PT_SC, PARAMS, TRIANGLE, VERTEX, default_params, material)
 
 __all__ = [
     "RTScene", "RTRenderer", "GbptError", "default_params", "material", "layouts",
-    "MODE_BDPT_SC", "MODE_BDPT_SC_ADAP_BILAT", "MODE_BDPT_SC_ADAP_BILAT_BINARY", "VERTEX", "TRIANGLE", "MATERIAL", "PARAMS",
+    "MODE_BDPT_SC", "MODE_BDPT_SC_ADAP_BILAT", "MODE_BDPT_SC_ADAP_BILAT_BINARY", "MODE_BDPT_SC_BILAT", "MODE_PT_SC",
+    "VERTEX",
+    "TRIANGLE", "MATERIAL", "PARAMS",
     "device_available", "camera",
 ]
 
@@ -148,6 +150,15 @@ class RTRenderer:
         return self._mode
 
     @property
+    def handle(self):
+        return self._h
+
+    def rmse(self, converged):
+        """RMSE of the current image against a converged W*H*3 image (on the GPU)."""
+        from .experiment import renderer_rmse
+        return renderer_rmse(self, converged)
+
+    @property
     def params(self):
         p = np.zeros((), PARAMS)
         check(load().gbpt_get_params(self._h, ptr(p)))
@@ -191,9 +202,10 @@ class RTRenderer:
         return self.last_stats
 
     def read_buffer(self, which):
-        """0 result, 1 position, 2 normal, 3 diffuse, 4 filtered, 5 error, 6 sample count."""
+        """0 result, 1 position, 2 normal, 3 diffuse, 4 filtered, 5 error, 6 sample count;
+        filter-only mode: 8 direct light, 9 first-hit emissive, 10 mean of 1 - path potential."""
         np_ = self.width * self.height
-        if which == 5:
+        if which in (5, 10):
             out = np.zeros(np_, np.float32)
         elif which == 6:
             out = np.zeros(np_, np.uint32)

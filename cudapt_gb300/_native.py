@@ -50,6 +50,7 @@ class Stats(ctypes.Structure):
         ("ms_shadow", ctypes.c_float),
         ("ms_filter", ctypes.c_float),
         ("ms_adapt", ctypes.c_float),
+        ("launches", ctypes.c_uint32),
     ]
 
     def as_dict(self):
@@ -88,6 +89,9 @@ SIGNATURES = {
     "gbpt_gaussian_table": (i32, [f32, u32, vp]),
     "gbpt_bilateral": (i32, [vp, vp, vp, vp, u32, u32, f32, f32, f32, f32, u32, vp, vp, i32]),
     "gbpt_bilateral_noalloc": (i32, [vp, vp, vp, vp, u32, u32, f32, f32, f32, f32, u32, vp, vp, vp]),
+    "gbpt_rmse": (i32, [vp, vp, ctypes.c_uint64, i32, vp]),
+    "gbpt_renderer_rmse": (i32, [vp, vp, i32, vp]),
+    "gbpt_tonemap_rgba8": (i32, [vp, vp, u32, u32, f32, i32, vp, i32]),
     "gbpt_fmath": (i32, [i32, vp, u32, vp]),
     "gbpt_philox": (i32, [vp, u32, u32, u32, vp]),
 }

@@ -182,6 +182,10 @@ struct gbpt_renderer {
   RenderBuffers rb{};
   AdaptBuffers ab{};
   float *result = nullptr, *gpos = nullptr, *gnorm = nullptr, *gdiff = nullptr, *gauss = nullptr;
+  // filter-only mode: first-hit emissive, direct-light and 1 - potential means,
+  // the second ping-pong filter plane and the "Prob" view scratch plane
+  float *gemis = nullptr, *direct = nullptr, *pot = nullptr, *filtered2 = nullptr, *probView = nullptr;
+  const float* bilatOut = nullptr;  // filter plane holding the last filtered image
   uint32_t* sampleN = nullptr;
   float4* waveMem = nullptr;
   std::vector<float> hostResult;
@@ -202,6 +206,7 @@ struct gbpt_renderer {
   uint64_t cacheEpoch[2] = {~0ull, ~0ull};
   uint32_t cacheFrame[2] = {0, 0};
   uint32_t lastSel = 0;
+  bool lastTraced = true;  // the last frame traced camera paths (filter-only mode may only filter)
 
   void free_dev() {
     for (int k = 0; k < 2; k++) rb.wave[k] = Wave{};
@@ -211,6 +216,7 @@ struct gbpt_renderer {
     dfree(rb.sh[1]);
     dfree(rb.res);
     dfree(rb.gbuf);
+    dfree(rb.dsm);
     dfree(rb.slotPix);
     dfree(rb.slotSmp);
     if (stLight) cudaStreamSynchronize(stLight);
@@ -230,6 +236,12 @@ struct gbpt_renderer {
     dfree(gpos);
     dfree(gnorm);
     dfree(gdiff);
+    dfree(gemis);
+    dfree(direct);
+    dfree(pot);
+    dfree(filtered2);
+    dfree(probView);
+    bilatOut = nullptr;
     dfree(gauss);
     dfree(sampleN);
     alloc = false;
@@ -255,6 +267,8 @@ gbpt_status check_params(const gbpt_params* p) {
   if (p->light_paths > 1024) return fail(GBPT_ERR_INVALID_ARG, "light_paths must be <= 1024");
   if (p->light_every < 1) return fail(GBPT_ERR_INVALID_ARG, "light_every must be >= 1");
   if (p->filter_radius > 31) return fail(GBPT_ERR_INVALID_ARG, "filter_radius must be <= 31");
+  if (p->bilat_radius > 31) return fail(GBPT_ERR_INVALID_ARG, "bilat_radius must be <= 31");
+  if (p->pt_depth_max < 1 || p->pt_depth_max > 64) return fail(GBPT_ERR_INVALID_ARG, "pt_depth_max must be 1..64");
   return GBPT_OK;
 }
 
@@ -264,7 +278,7 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   const size_t cap = np;
   const uint32_t cacheCap = std::max(1u, r->p.light_paths * (1 + r->p.light_depth_max));
   // admission: refuse when the buffers cannot fit in free HBM
-  size_t need = cap * (128 + 16 + 96 + 16 + 48 + 8) + np * (12 * 5 + 4 + 4 * 4) + (size_t)cacheCap * 192;
+  size_t need = cap * (128 + 16 + 96 + 16 + 48 + 16 + 8) + np * (12 * 10 + 4 * 2 + 4 * 4) + (size_t)cacheCap * 192;
   size_t freeB = 0, totB = 0;
   CK(cudaMemGetInfo(&freeB, &totB));
   if (need + (64ull << 20) > freeB)
@@ -280,6 +294,7 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   CK(dalloc(&r->rb.sh[1], cap * 3));
   CK(dalloc(&r->rb.res, cap));
   CK(dalloc(&r->rb.gbuf, cap * 3));
+  CK(dalloc(&r->rb.dsm, cap));
   CK(dalloc(&r->rb.slotPix, cap));
   CK(dalloc(&r->rb.slotSmp, cap));
   CK(dalloc(&r->rb.cache[0], (size_t)cacheCap * 6));
@@ -294,6 +309,11 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   CK(dalloc(&r->gpos, np * 3));
   CK(dalloc(&r->gnorm, np * 3));
   CK(dalloc(&r->gdiff, np * 3));
+  CK(dalloc(&r->gemis, np * 3));
+  CK(dalloc(&r->direct, np * 3));
+  CK(dalloc(&r->pot, np));
+  CK(dalloc(&r->filtered2, np * 3));
+  CK(dalloc(&r->probView, np * 3));
   CK(dalloc(&r->sampleN, np));
   CK(dalloc(&r->gauss, 64));
   CK(dalloc(&r->ab.err, np));
@@ -304,8 +324,11 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   CK(dalloc(&r->ab.filtered, np * 3));
   CK(dalloc(&r->ab.coop, kCoopWords));
   CK(cudaMemsetAsync(r->ab.coop, 0, kCoopWords * 4, r->st));
-  for (float* b : {r->result, r->gpos, r->gnorm, r->gdiff, r->ab.filtered})
+  for (float* b : {r->result, r->gpos, r->gnorm, r->gdiff, r->ab.filtered, r->gemis, r->direct, r->filtered2,
+                   r->probView})
     CK(cudaMemsetAsync(b, 0, np * 12, r->st));
+  CK(cudaMemsetAsync(r->pot, 0, np * 4, r->st));
+  r->bilatOut = r->ab.filtered;
   CK(cudaMemsetAsync(r->sampleN, 0, np * 4, r->st));
   CK(cudaMemsetAsync(r->ab.err, 0, np * 4, r->st));
   r->hostResult.assign(np * 3, 0.f);
@@ -349,6 +372,47 @@ cudaEvent_t mark(gbpt_renderer* r, int phase, bool timing) {
   return e;
 }
 
+gbpt_status ensure_gauss(gbpt_renderer* r, float delta, uint32_t radius, cudaStream_t st) {
+  if (r->gaussKey[0] != delta || r->gaussKey[1] != (float)radius) {
+    float g[64] = {0};
+    gaussian_table_host(delta, radius, g);
+    CK(cudaMemcpyAsync(r->gauss, g, sizeof(g), cudaMemcpyHostToDevice, st));
+    r->gaussKey[0] = delta;
+    r->gaussKey[1] = (float)radius;
+  }
+  return GBPT_OK;
+}
+
+// Filter stage of the filter-only mode (src/cudaRTBDPTStreamBilat.cu:1418-1432):
+// posnormemit with the first-hit diffuse plane as the third feature, then
+// "Filter Iteration" - 1 more passes ping-ponging between two planes.  Debug
+// modes 2/3 filter the path-potential view instead of the result (the
+// reference overwrites its accumulator with that view; here it stays intact).
+gbpt_status bilat_filter(gbpt_renderer* r, cudaStream_t st, bool timing) {
+  const gbpt_params& p = r->p;
+  const float delta = p.filter_sigma_spatial > 0.f ? p.filter_sigma_spatial : p.bilat_color_eud;
+  gbpt_status e = ensure_gauss(r, delta, p.bilat_radius, st);
+  if (e != GBPT_OK) return e;
+  const float* src = r->result;
+  const int dm = (int)r->debugMode;
+  if (dm == 2 || dm == 3) {
+    CK(launch_prob_view(r->pot, r->W * r->H, dm == 3 ? p.min_trace_prob : 0.f, r->probView, st));
+    src = r->probView;
+  }
+  float* planes[2] = {r->ab.filtered, r->filtered2};
+  int cur = 0;
+  CK(launch_bilateral(src, r->gpos, r->gnorm, r->gdiff, r->W, r->H, p.bilat_color_eud, p.bilat_pos_eud,
+                      p.bilat_norm_eud, p.bilat_diff_eud, p.bilat_radius, r->gauss, planes[cur], st));
+  for (uint32_t i = 1; i < p.filter_iterations; i++) {
+    CK(launch_bilateral(planes[cur], r->gpos, r->gnorm, r->gdiff, r->W, r->H, p.bilat_color_eud, p.bilat_pos_eud,
+                        p.bilat_norm_eud, p.bilat_diff_eud, p.bilat_radius, r->gauss, planes[cur ^ 1], st));
+    cur ^= 1;
+  }
+  r->bilatOut = planes[cur];
+  mark(r, kPhFilter, timing);
+  return GBPT_OK;
+}
+
 gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, bool timing) {
   float right[3], up[3];
   cam_basis(*cam, right, up);
@@ -376,7 +440,9 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   a.frame = r->frame;
   a.key0 = r->p.seed;
   a.key1 = r->p.request_id;
-  a.eyeDepth = r->p.eye_depth_max;
+  const bool pt = r->mode == GBPT_MODE_PT_SC;  // unidirectional: no light pass, no connections
+  a.ptsc = pt ? 1u : 0u;
+  a.eyeDepth = pt ? r->p.pt_depth_max : r->p.eye_depth_max;
   a.lightDepth = r->p.light_depth_max;
   a.lightPaths = r->p.light_paths;
   for (int k = 0; k < 3; k++) a.env[k] = r->p.env[k];
@@ -385,10 +451,18 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   const bool binary = r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY;
   // the PLL variant pushes the specular origin along reflDir (AdapBilatAtomic.cu:583); the others do not
   a.specPush = r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT ? 1u : 0u;
-  a.gbuffer = adaptive ? 1u : 0u;
+  const bool bilat = r->mode == GBPT_MODE_BDPT_SC_BILAT;
+  a.gbuffer = (adaptive || bilat) ? 1u : 0u;
+  a.bilat = bilat ? 1u : 0u;
   a.counting = r->counting ? 1u : 0u;
   const DevScene& S = s->dev;
   cudaStream_t st = r->st;
+  // filter-only mode: frames past "Render Iteration" trace nothing and only
+  // filter again (src/cudaRTBDPTStreamBilat.cu:1278)
+  const uint32_t RI = r->p.render_iterations;
+  auto traces = [&](uint32_t f) { return !bilat || RI == 0 || f < RI; };
+  r->lastTraced = traces(r->frame);
+  if (!r->lastTraced) return bilat_filter(r, st, timing);
 
   mark(r, kPhOther, timing);
   // light pass (src/cudaRTBDPTStream.cu:875-906): group g = frame / light_every
@@ -399,7 +473,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   const uint32_t sel = g & 1u;
   a.cacheSel = sel;
   r->lastSel = sel;
-  if (r->frame % k == 0) {
+  if (!pt && r->frame % k == 0) {
     const bool ready = r->cacheEpoch[sel] == r->epoch && r->cacheFrame[sel] == r->frame;
     if (r->lightPending[sel]) CK(cudaStreamWaitEvent(st, r->evLight[sel], 0));
     r->lightPending[sel] = false;
@@ -412,27 +486,24 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
     // run the next group's light pass ahead, into the other cache: it waits
     // for everything queued so far (earlier frames that read that cache)
     const uint32_t nsel = sel ^ 1u;
-    CK(cudaEventRecord(r->evMain, st));
-    CK(cudaStreamWaitEvent(r->stLight, r->evMain, 0));
-    FrameArgs an = a;
-    an.frame = r->frame + k;
-    an.cacheSel = nsel;
-    CK(launch_light_pass(S, an, r->rb, r->stLight));
-    CK(cudaEventRecord(r->evLight[nsel], r->stLight));
-    r->lightPending[nsel] = true;
-    r->cacheEpoch[nsel] = r->epoch;
-    r->cacheFrame[nsel] = r->frame + k;
+    if (traces(r->frame + k)) {
+      CK(cudaEventRecord(r->evMain, st));
+      CK(cudaStreamWaitEvent(r->stLight, r->evMain, 0));
+      FrameArgs an = a;
+      an.frame = r->frame + k;
+      an.cacheSel = nsel;
+      CK(launch_light_pass(S, an, r->rb, r->stLight));
+      CK(cudaEventRecord(r->evLight[nsel], r->stLight));
+      r->lightPending[nsel] = true;
+      r->cacheEpoch[nsel] = r->epoch;
+      r->cacheFrame[nsel] = r->frame + k;
+    }
   }
   const bool budgeted = adaptive && r->frame >= r->p.warmup_frames;
   if (budgeted) {
     float delta = r->p.filter_sigma_spatial > 0.f ? r->p.filter_sigma_spatial : r->p.filter_color_eud;
-    if (r->gaussKey[0] != delta || r->gaussKey[1] != (float)r->p.filter_radius) {
-      float g[64] = {0};
-      gaussian_table_host(delta, r->p.filter_radius, g);
-      CK(cudaMemcpyAsync(r->gauss, g, sizeof(g), cudaMemcpyHostToDevice, st));
-      r->gaussKey[0] = delta;
-      r->gaussKey[1] = (float)r->p.filter_radius;
-    }
+    gbpt_status ge = ensure_gauss(r, delta, r->p.filter_radius, st);
+    if (ge != GBPT_OK) return ge;
     CK(launch_bilateral(r->result, r->gpos, r->gnorm, r->p.filter_diffuse ? r->gdiff : nullptr, r->W, r->H,
                         r->p.filter_color_eud, r->p.filter_pos_eud, r->p.filter_norm_eud, r->p.filter_diff_eud,
                         r->p.filter_radius, r->gauss, r->ab.filtered, st));
@@ -451,10 +522,10 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   // every remaining path to its end (few paths are left by then, and per-bounce
   // launches would each wait for their slowest ray)
   int in = 0;
-  const uint32_t D = r->p.eye_depth_max;
+  const uint32_t D = a.eyeDepth;
   const uint32_t K = std::min(tail_from(D), D);
   for (uint32_t d = 0; d < K; d++) {
-    CK(launch_walk(S, a, r->rb, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), st));
+    CK(launch_walk(S, a, r->rb, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), d == 1, st));
     mark(r, kPhTrace, timing);
     CK(launch_shade(S, a, r->rb, in, d, K < D && d + 1 == K, st));
     mark(r, kPhShade, timing);
@@ -465,7 +536,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   } else {
     // shadow rays of the last bounce (none in practice: paths at the depth cap
     // terminate without connecting; kept so the sequence needs no special case)
-    CK(launch_walk(S, a, r->rb, -1, (int)((D - 1) & 1u), (int)(D & 1u), st));
+    CK(launch_walk(S, a, r->rb, -1, (int)((D - 1) & 1u), (int)(D & 1u), D == 1, st));
   }
   mark(r, kPhTrace, timing);
   if (budgeted) {
@@ -474,6 +545,14 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
     else
       CK(launch_adapt_accum(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
     mark(r, kPhAdapt, timing);
+  } else if (pt) {
+    CK(launch_apply_pt(a, r->rb, r->result, r->sampleN, st));
+    mark(r, kPhOther, timing);
+  } else if (bilat) {
+    CK(launch_apply_bilat(a, r->rb, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, r->gemis, r->direct, r->pot,
+                          st));
+    mark(r, kPhOther, timing);
+    return bilat_filter(r, st, timing);
   } else {
     CK(launch_apply(a, r->rb, r->result, r->sampleN, adaptive ? r->gpos : nullptr, r->gnorm, r->gdiff, st));
     mark(r, kPhOther, timing);
@@ -491,6 +570,15 @@ gbpt_status read_ctr(gbpt_renderer* r, DevCounters* out) {
   return GBPT_OK;
 }
 
+// The image gbpt_render copies out: the result, or the mode's debug view.
+const float* output_view(const gbpt_renderer* r) {
+  if (r->mode == GBPT_MODE_BDPT_SC_BILAT) {  // src/cudaRTBDPTStreamBilat.cu:1440-1459
+    const int dm = (int)r->debugMode;
+    return dm == 4 ? r->direct : dm == 5 ? r->gpos : dm == 6 ? r->gnorm : dm == 7 ? r->result : r->bilatOut;
+  }
+  return (r->debugMode == 4.f && r->mode != GBPT_MODE_BDPT_SC) ? r->ab.filtered : r->result;
+}
+
 gbpt_status render_impl(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, uint32_t frames, float* out,
                         int32_t outDev, gbpt_stats* stats) {
   if (!r || !s || !cam) return fail(GBPT_ERR_INVALID_ARG, "NULL renderer, scene or camera");
@@ -504,16 +592,15 @@ gbpt_status render_impl(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam,
     stt = read_ctr(r, &before);
     if (stt != GBPT_OK) return stt;
   }
+  const uint64_t launches0 = launch_count();
   r->evs.clear();
   for (uint32_t f = 0; f < frames; f++) {
     stt = frame_once(r, s, cam, timing);
     if (stt != GBPT_OK) return stt;
   }
   const size_t np = (size_t)r->W * r->H;
-  if (out) {
-    const float* src = (r->debugMode == 4.f && r->mode != GBPT_MODE_BDPT_SC) ? r->ab.filtered : r->result;
-    CK(cudaMemcpyAsync(out, src, np * 12, outDev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, r->st));
-  }
+  if (out) CK(cudaMemcpyAsync(out, output_view(r), np * 12, outDev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                             r->st));
   CK(cudaStreamSynchronize(r->st));
   CK(cudaGetLastError());
   {  // device-side error words (bounded waits, bounds checks): report once, then clear
@@ -531,8 +618,8 @@ gbpt_status render_impl(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam,
     if (stt != GBPT_OK) return stt;
     std::memset(stats, 0, sizeof(*stats));
     stats->frame = r->frame;
-    stats->light_vertices = after.cacheSize[r->lastSel];
-    stats->paths = after.paths;
+    stats->light_vertices = r->mode == GBPT_MODE_PT_SC ? 0u : after.cacheSize[r->lastSel];
+    stats->paths = r->lastTraced ? after.paths : 0;
     stats->rays = after.rays - before.rays;
     stats->nodes = after.nodes - before.nodes;
     stats->tris = after.tris - before.tris;
@@ -552,13 +639,14 @@ gbpt_status render_impl(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam,
     stats->ms_shadow = ph[kPhShadow];
     stats->ms_filter = ph[kPhFilter];
     stats->ms_adapt = ph[kPhAdapt];
+    stats->launches = (uint32_t)(launch_count() - launches0);
   }
   return GBPT_OK;
 }
 
 struct AttrDef {
   const char* name;
-  int kind;  // 0 float, 1 uint
+  int kind;  // 0 float, 1 uint, 2 the renderer's debug view
   size_t off;
 };
 // reference attribute names first (src/cudaRTBDPTStreamAdapBilatAtomic.cu:48-60)
@@ -578,8 +666,48 @@ const AttrDef kAttrs[] = {
     {"Filter Sigma Spatial", 0, offsetof(gbpt_params, filter_sigma_spatial)},
     {"Seed", 1, offsetof(gbpt_params, seed)},
     {"Min Trace Probability", 0, offsetof(gbpt_params, min_trace_prob)},
+    {"Debug Mode", 2, 0},
 };
 constexpr uint32_t kAttrN = sizeof(kAttrs) / sizeof(kAttrs[0]);
+// "BDPTSC Bilaterial" (src/cudaRTBDPTStreamBilat.cu:40-50), then the defines
+const AttrDef kAttrsBilat[] = {
+    {"Filter Color E Delta", 0, offsetof(gbpt_params, bilat_color_eud)},
+    {"Filter Pos E Delta", 0, offsetof(gbpt_params, bilat_pos_eud)},
+    {"Filter Norm E Delta", 0, offsetof(gbpt_params, bilat_norm_eud)},
+    {"Filter Emit E Delta", 0, offsetof(gbpt_params, bilat_emit_eud)},
+    {"Filter Diff E Delta", 0, offsetof(gbpt_params, bilat_diff_eud)},
+    {"Filter Radius", 1, offsetof(gbpt_params, bilat_radius)},
+    {"Filter Iteration", 1, offsetof(gbpt_params, filter_iterations)},
+    {"Debug Mode", 2, 0},
+    {"Render Iteration", 1, offsetof(gbpt_params, render_iterations)},
+    {"Eye Depth Max", 1, offsetof(gbpt_params, eye_depth_max)},
+    {"Light Depth Max", 1, offsetof(gbpt_params, light_depth_max)},
+    {"Light Paths", 1, offsetof(gbpt_params, light_paths)},
+    {"Light Pass Every", 1, offsetof(gbpt_params, light_every)},
+    {"Filter Sigma Spatial", 0, offsetof(gbpt_params, filter_sigma_spatial)},
+    {"Seed", 1, offsetof(gbpt_params, seed)},
+    {"MinTraceProb", 0, offsetof(gbpt_params, min_trace_prob)},
+};
+constexpr uint32_t kAttrBilatN = sizeof(kAttrsBilat) / sizeof(kAttrsBilat[0]);
+// "PTSC" has no attributes in the reference (src/cudaRTPTStream.cu:10); its define and the seed
+const AttrDef kAttrsPT[] = {
+    {"PT Depth Max", 1, offsetof(gbpt_params, pt_depth_max)},
+    {"Seed", 1, offsetof(gbpt_params, seed)},
+};
+constexpr uint32_t kAttrPTN = sizeof(kAttrsPT) / sizeof(kAttrsPT[0]);
+
+const AttrDef* attr_table(const gbpt_renderer* r, uint32_t* n) {
+  if (r->mode == GBPT_MODE_BDPT_SC_BILAT) {
+    *n = kAttrBilatN;
+    return kAttrsBilat;
+  }
+  if (r->mode == GBPT_MODE_PT_SC) {
+    *n = kAttrPTN;
+    return kAttrsPT;
+  }
+  *n = kAttrN;
+  return kAttrs;
+}
 
 }  // namespace
 
@@ -624,6 +752,15 @@ gbpt_status gbpt_params_default(gbpt_params* p) {
   p->filter_sigma_spatial = 0.f;
   p->request_id = 0;
   p->min_trace_prob = 0.f;
+  p->bilat_color_eud = 1.f;
+  p->bilat_pos_eud = 1.f;
+  p->bilat_norm_eud = 1.f;
+  p->bilat_emit_eud = 0.5f;
+  p->bilat_diff_eud = 0.5f;
+  p->bilat_radius = 5;
+  p->filter_iterations = 1;
+  p->render_iterations = 5;
+  p->pt_depth_max = 10;
   return GBPT_OK;
 }
 
@@ -762,7 +899,7 @@ gbpt_status gbpt_renderer_create(uint32_t width, uint32_t height, int32_t mode, 
   *out = nullptr;
   if (width == 0 || height == 0 || (uint64_t)width * height > (1ull << 26))
     return fail(GBPT_ERR_INVALID_ARG, "image size must be 1..2^26 pixels");
-  if (mode < GBPT_MODE_BDPT_SC || mode > GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY)
+  if (mode < GBPT_MODE_BDPT_SC || mode > GBPT_MODE_PT_SC)
     return fail(GBPT_ERR_INVALID_ARG, "unknown renderer mode");
   gbpt_params p;
   if (params) {
@@ -860,9 +997,12 @@ gbpt_status gbpt_read_buffer(gbpt_renderer* r, int32_t which, void* dst, size_t 
     case 1: src = r->gpos; break;
     case 2: src = r->gnorm; break;
     case 3: src = r->gdiff; break;
-    case 4: src = r->ab.filtered; break;
+    case 4: src = r->mode == GBPT_MODE_BDPT_SC_BILAT ? r->bilatOut : r->ab.filtered; break;
     case 5: src = r->ab.err; need = np * 4; break;
     case 6: src = r->sampleN; need = np * 4; break;
+    case 8: src = r->direct; break;
+    case 9: src = r->gemis; break;
+    case 10: src = r->pot; need = np * 4; break;
     case 7: {  // light-vertex cache in the 21-float layout of the reference's LightVertex
       DevCounters c{};
       gbpt_status st = read_ctr(r, &c);
@@ -897,6 +1037,21 @@ gbpt_status gbpt_read_buffer(gbpt_renderer* r, int32_t which, void* dst, size_t 
   return GBPT_OK;
 }
 
+gbpt_status gbpt_renderer_rmse(gbpt_renderer* r, const float* converged, int32_t converged_is_device, double* out) {
+  if (!r || !converged || !out) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  if (!r->alloc) return fail(GBPT_ERR_STATE, "renderer has not rendered yet");
+  const size_t n = (size_t)r->W * r->H * 3;
+  if (converged_is_device) return rmse_device(output_view(r), converged, n, out, r->st);
+  float* d = nullptr;
+  CK(dalloc(&d, n));
+  cudaError_t e = cudaMemcpyAsync(d, converged, n * 4, cudaMemcpyHostToDevice, r->st);
+  gbpt_status st = e == cudaSuccess ? rmse_device(output_view(r), d, n, out, r->st)
+                                    : fail(GBPT_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+  cudaStreamSynchronize(r->st);
+  dfree(d);
+  return st;
+}
+
 gbpt_status gbpt_reset(gbpt_renderer* r) {
   if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
   r->started = false;
@@ -919,38 +1074,34 @@ gbpt_status gbpt_set_counting(gbpt_renderer* r, int32_t on) {
 
 gbpt_status gbpt_attr_count(const gbpt_renderer* r, uint32_t* n) {
   if (!r || !n) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
-  *n = kAttrN + 1;
+  attr_table(r, n);
   return GBPT_OK;
 }
 
 gbpt_status gbpt_attr_name(const gbpt_renderer* r, uint32_t index, char* name, size_t cap) {
   if (!r || !name || cap == 0) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
-  const char* nm = nullptr;
-  if (index < kAttrN)
-    nm = kAttrs[index].name;
-  else if (index == kAttrN)
-    nm = "Debug Mode";
-  else
-    return fail(GBPT_ERR_INVALID_ARG, "attribute index out of range");
-  std::strncpy(name, nm, cap - 1);
+  uint32_t n = 0;
+  const AttrDef* t = attr_table(r, &n);
+  if (index >= n) return fail(GBPT_ERR_INVALID_ARG, "attribute index out of range");
+  std::strncpy(name, t[index].name, cap - 1);
   name[cap - 1] = 0;
   return GBPT_OK;
 }
 
 gbpt_status gbpt_attr_get(const gbpt_renderer* r, const char* name, float* value) {
   if (!r || !name || !value) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
-  if (std::strcmp(name, "Debug Mode") == 0) {
-    *value = r->debugMode;
-    return GBPT_OK;
-  }
-  for (uint32_t i = 0; i < kAttrN; i++)
-    if (std::strcmp(name, kAttrs[i].name) == 0) {
+  uint32_t n = 0;
+  const AttrDef* t = attr_table(r, &n);
+  for (uint32_t i = 0; i < n; i++)
+    if (std::strcmp(name, t[i].name) == 0) {
       const char* base = (const char*)&r->p;
-      if (kAttrs[i].kind == 0)
-        std::memcpy(value, base + kAttrs[i].off, 4);
-      else {
+      if (t[i].kind == 2) {
+        *value = r->debugMode;
+      } else if (t[i].kind == 0) {
+        std::memcpy(value, base + t[i].off, 4);
+      } else {
         uint32_t u;
-        std::memcpy(&u, base + kAttrs[i].off, 4);
+        std::memcpy(&u, base + t[i].off, 4);
         *value = (float)u;
       }
       return GBPT_OK;
@@ -960,21 +1111,29 @@ gbpt_status gbpt_attr_get(const gbpt_renderer* r, const char* name, float* value
 
 gbpt_status gbpt_attr_set(gbpt_renderer* r, const char* name, float value) {
   if (!r || !name) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
-  if (std::strcmp(name, "Debug Mode") == 0) {
-    if (value != 0.f && value != 4.f) return fail(GBPT_ERR_INVALID_ARG, "Debug Mode supports 0 (None) and 4 (Filtered)");
-    r->debugMode = value;
-    return GBPT_OK;
-  }
-  for (uint32_t i = 0; i < kAttrN; i++)
-    if (std::strcmp(name, kAttrs[i].name) == 0) {
+  uint32_t n = 0;
+  const AttrDef* t = attr_table(r, &n);
+  for (uint32_t i = 0; i < n; i++)
+    if (std::strcmp(name, t[i].name) == 0) {
+      if (t[i].kind == 2) {
+        if (r->mode == GBPT_MODE_BDPT_SC_BILAT) {
+          // None, Traced, Prob, Prob With Limit, Direct, Position, Normal, Non-Filter (:27)
+          if (!(value >= 0.f && value <= 7.f) || value != (float)(int)value)
+            return fail(GBPT_ERR_INVALID_ARG, "Debug Mode is 0..7 in BDPTSC Bilaterial");
+        } else if (value != 0.f && value != 4.f) {
+          return fail(GBPT_ERR_INVALID_ARG, "Debug Mode supports 0 (None) and 4 (Filtered)");
+        }
+        r->debugMode = value;
+        return GBPT_OK;
+      }
       gbpt_params p = r->p;
       char* base = (char*)&p;
-      if (kAttrs[i].kind == 0) {
-        std::memcpy(base + kAttrs[i].off, &value, 4);
+      if (t[i].kind == 0) {
+        std::memcpy(base + t[i].off, &value, 4);
       } else {
         if (!(value >= 0.f) || value > 4294967295.f) return fail(GBPT_ERR_INVALID_ARG, "value out of range");
         uint32_t u = (uint32_t)value;
-        std::memcpy(base + kAttrs[i].off, &u, 4);
+        std::memcpy(base + t[i].off, &u, 4);
       }
       return gbpt_set_params(r, &p);
     }

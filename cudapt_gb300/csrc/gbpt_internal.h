@@ -20,6 +20,10 @@ struct HostBVH {
 bool build_bvh(const gbpt_vertex* verts, const gbpt_triangle* tris, uint32_t nt, uint32_t maxDepth, uint32_t threads,
                HostBVH* out);
 
+// sqrt(mean((a - b)^2)) over n floats in device memory, summed in double on
+// `stream` (a cudaStream_t); image.cu
+gbpt_status rmse_device(const float* a, const float* b, uint64_t n, double* out, void* stream);
+
 // thread-local error text (gbpt_last_error_string)
 void set_error(const std::string& s);
 gbpt_status fail(gbpt_status st, const std::string& s);

@@ -624,6 +624,7 @@ cudaError_t launch_bilateral(const float* color, const float* pos, const float* 
   } else {
     k_bilateral_direct<false><<<grid, block, 0, st>>>(color, pos, norm, emit, W, H, cc2, pc2, nc2, ec2, r, g, out);
   }
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -637,6 +638,7 @@ cudaError_t launch_adapt_budget(const FrameArgs& a, const RenderBuffers& b, cons
   k_scan_blocks<<<1, 1024, 0, st>>>(ab.blockSum, ns, np, b.ctr);
   k_offsets<<<(np + 255) / 256, 256, 0, st>>>(ab.off, ab.cnt, ab.blockSum, np, np);
   k_gen_adapt<<<sm_count() * 8, 256, 0, st>>>(a, b, ab.off, ab.cnt);
+  note_launches(6);
   return cudaGetLastError();
 }
 
@@ -645,6 +647,7 @@ cudaError_t launch_adapt_accum(const FrameArgs& a, const RenderBuffers& b, const
   const uint32_t np = a.width * a.height;
   k_accum<<<(uint32_t)(((size_t)np * 32 + 255) / 256), 256, 0, st>>>(a, b, ab.off, ab.cnt, result, sampleN, gpos,
                                                                      gnorm, gdiff);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -675,6 +678,7 @@ cudaError_t launch_binary_budget(const FrameArgs& a, const RenderBuffers& b, con
   e = cudaLaunchCooperativeKernel((const void*)k_bin_search, dim3(g), dim3(256), args, 0, st);
   if (e != cudaSuccess) return e;
   k_gen_queue<<<(np + 255) / 256, 256, 0, st>>>(a, b, np);
+  note_launches(3);
   return cudaGetLastError();
 }
 
@@ -687,16 +691,19 @@ cudaError_t launch_binary_apply(const FrameArgs& a, const RenderBuffers& b, cons
   RenderBuffers bb = b;
   uint32_t* coop = ab.coop;
   void* args[] = {&aa, &bb, &coop, &result, &sampleN, &gpos, &gnorm, &gdiff};
+  note_launches(1);
   return cudaLaunchCooperativeKernel((const void*)k_bin_apply, dim3(g), dim3(256), args, 0, st);
 }
 
 cudaError_t launch_fmath(int which, const float* x, uint32_t n, float* out, cudaStream_t st) {
   if (n) k_fmath<<<(n + 255) / 256, 256, 0, st>>>(which, x, n, out);
+  if (n) note_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_philox(const uint32_t* ctr, uint32_t n, uint32_t k0, uint32_t k1, uint32_t* out, cudaStream_t st) {
   if (n) k_philox<<<(n + 255) / 256, 256, 0, st>>>(ctr, n, k0, k1, out);
+  if (n) note_launches(1);
   return cudaGetLastError();
 }
 

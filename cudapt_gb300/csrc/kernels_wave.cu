@@ -20,6 +20,7 @@
 //
 // Queue lengths live in device memory (DevCounters) and every kernel runs a
 // grid-stride loop over them, so the host never waits on a count.
+#include <atomic>
 #include <cuda_runtime.h>
 
 #include <cstdlib>
@@ -88,12 +89,22 @@ enum : uint32_t { kTypeEye = 0, kTypeDiff = 1, kTypeSpec = 2, kTypeLight = 3 };
 
 // The bounce decision shared by eye and light paths (reflect / transmit /
 // diffuse, src/cudaRTBDPTStream.cu:400-493 and :223-323).
+// With wantPdf, also the sampling density of the filter-only variant
+// (src/cudaRTBDPTStreamBilat.cu:515-518, :560, :575, :599): D*NoH/(4 VoH)
+// times the probability of the branch taken.
 struct Bounce {
   f3 nl, nOrig, nDir, lmt, F;
   uint32_t type;
+  float pdf;
 };
+//
+// ptTir: the unidirectional variant reflects on total internal reflection
+// (src/cudaRTPTStream.cu:153-160: cos2t < 0 sets reflProb = 1); the BDPT
+// variants compute the refracted direction regardless (the test is commented
+// out there).  The refracted direction stays zero when it is not computed
+// (uninitialised in the reference).
 __device__ __forceinline__ void sample_bounce(f3 orig, f3 dir, float dist, f3 norm, const Mat& m, const float* u,
-                                              bool specPush, Bounce& B) {
+                                              bool specPush, bool wantPdf, bool ptTir, Bounce& B) {
   using namespace gb;
   B.nl = dot(norm, dir) < 0.f ? norm : -1.f * norm;
   const f3 nl = B.nl;
@@ -103,6 +114,11 @@ __device__ __forceinline__ void sample_bounce(f3 orig, f3 dir, float dist, f3 no
   f3 f0 = vlerp(kF0Spec * mk(m.spec, m.spec, m.spec), m.diff, m.metal);
   f3 F = f_schlick(f0, voH);
   B.F = F;
+  B.pdf = 1.f;
+  if (wantPdf) {
+    const float NoH0 = dot(nl, hDir);
+    B.pdf = (d_ggx(m.rough, NoH0) * NoH0) / (4.f * voH);
+  }
   float reflProb = lerp(length(F), 1.0f, m.metal);
   float refrProb = m.trans;
   f3 reflDir = mk(0.f, 0.f, 0.f), refrDir = reflDir;
@@ -112,7 +128,10 @@ __device__ __forceinline__ void sample_bounce(f3 orig, f3 dir, float dist, f3 no
     float nnt = into ? 1.0f / nt : nt / 1.0f;
     float ddn = dot(hDir, dir);
     float cos2t = 1.f - (nnt * nnt) * (1.f - ddn * ddn);
-    refrDir = normalize(dir * nnt - hDir * (ddn * nnt + sqrtf(cos2t)));
+    if (ptTir && cos2t < 0.f)
+      reflProb = 1.0f;
+    else
+      refrDir = normalize(dir * nnt - hDir * (ddn * nnt + sqrtf(cos2t)));
   }
   if (reflProb > 0.f) {
     reflDir = normalize(dir - (hDir * 2.f) * dot(hDir, dir));
@@ -126,18 +145,21 @@ __device__ __forceinline__ void sample_bounce(f3 orig, f3 dir, float dist, f3 no
     float G = vis_smith(m.rough, NoV, NoL);
     B.lmt = ((F * G) * VoH) / ((NoV * NoH) * reflProb);
     B.type = kTypeSpec;
+    B.pdf = B.pdf * reflProb;
   } else if (prob_rand(refrProb, u[3])) {
     B.nOrig = (orig + (dist + kBias) * dir) + refrDir * kBias;
     B.nDir = refrDir;
     float cosine = dot(-1.f * nl, refrDir);
     B.lmt = (cosine * m.diff) / (refrProb * (1.f - reflProb));
     B.type = kTypeSpec;
+    B.pdf = B.pdf * (refrProb * (1.f - reflProb));
   } else {
     f3 dd = cos_dir(u[4], u[5], nl);
     B.nOrig = (orig + dist * dir) + dd * kBias;
     B.nDir = dd;
     B.lmt = (kPi * (m.diff * kInvPi)) / ((1.f - refrProb) * (1.f - reflProb));
     B.type = kTypeDiff;
+    B.pdf = B.pdf * (((1.f - refrProb) * (1.f - reflProb)) * dot(dd, nl));
   }
 }
 
@@ -247,7 +269,7 @@ __global__ void __launch_bounds__(1024) k_light(DevScene S, FrameArgs a, float4*
           Surf sf = load_surf(S, h.tri, hw, h.u, h.v, true);
           Mat m = load_mat(S, sf.mat);
           Bounce B;
-          sample_bounce(orig, dir, h.t, sf.norm, m, u, false, B);
+          sample_bounce(orig, dir, h.t, sf.norm, m, u, false, false, false, B);
           LV v;
           v.irrad = (B.type != kTypeDiff) ? mk(0.f, 0.f, 0.f) : sample;
           v.irradDir = -1.f * dir;
@@ -306,7 +328,7 @@ __global__ void k_camera(FrameArgs a, RenderBuffers b) {
   Wave w = b.wave[0];
   w.o[p] = make_float4(a.camPos[0], a.camPos[1], a.camPos[2], __uint_as_float(p));
   w.d[p] = st4u(dir, p);
-  w.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+  w.thr[p] = make_float4(1.f, 1.f, 1.f, 1.f);  // .w: path potential (filter-only mode)
   w.smp[p] = make_float4(0.f, 0.f, 0.f, 0.f);
   b.res[p] = make_float4(0.f, 0.f, 0.f, __uint_as_float(0u));
   b.slotPix[p] = p;
@@ -316,6 +338,18 @@ __global__ void k_camera(FrameArgs a, RenderBuffers b) {
     b.gbuf[3 * (size_t)p + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
     b.gbuf[3 * (size_t)p + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
+  if (a.bilat) b.dsm[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Direct-light sample of a bounce-0 connection that reached its light vertex
+// (pt_connectEyeLightPath_kernel, src/cudaRTBDPTStreamBilat.cu:905-913):
+// (direct + L) / 5 when any channel is positive, else L / 4.
+__device__ __forceinline__ void direct_connect(float4* dsm, uint32_t slot, float4 C) {
+  using namespace gb;
+  const float4 q = dsm[slot];
+  const f3 L = ld3(C);
+  const f3 d = (q.x > 0.f || q.y > 0.f || q.z > 0.f) ? (ld3(q) + L) / 5.f : L / 4.f;
+  dsm[slot] = st4(d, q.w);
 }
 
 __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, uint32_t v) {
@@ -335,9 +369,9 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, uint32_t v
 // results do not depend on this scheduling.  The any-hit walk stops at the
 // first hit closer than maxDist: that is exactly when the reference's
 // closest-hit walk with the same maxDist would report a hit.
-template <bool kCount>
-__global__ void __launch_bounds__(kBlock) k_walk(DevScene S, RenderBuffers b, int in, int shIn, int shReset,
-                                                 uint32_t kRefill) {
+template <bool kCount, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_walk(DevScene S, RenderBuffers b, int in, int shIn, int shReset,
+                                                 uint32_t shDirect, uint32_t kRefill) {
   const uint32_t nE = (in >= 0) ? b.ctr->wave[in] : 0u;
   const uint32_t nS = (shIn >= 0) ? b.ctr->shadow[shIn] : 0u;
   const uint32_t n = nE + nS;
@@ -388,6 +422,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(DevScene S, RenderBuffers b, in
           const float4 r = b.res[slot];
           b.res[slot] =
               make_float4(r.x + C.x, r.y + C.y, r.z + C.z, __uint_as_float(__float_as_uint(r.w) + 4u));
+          if (shDirect) direct_connect(b.dsm, slot, C);
         }
       } else {
         b.hit[item] = w.hit() ? make_float4(w.minT, __uint_as_float(w.best), w.bu, w.bv)
@@ -425,11 +460,13 @@ __device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a
   const uint32_t slot = __float_as_uint(io.o.w);
   const uint32_t pix = __float_as_uint(io.d.w);
   f3 orig = ld3(io.o), dir = ld3(io.d), outMul = ld3(io.t), pathSample = ld3(io.s);
+  float pot = io.t.w;  // path potential (filter-only mode)
   if (h4.x < 0.f) {  // miss (:537-542), plus the optional environment term
     if (a.useEnv) pathSample = pathSample + vmul(mk(a.env[0], a.env[1], a.env[2]), outMul);
     const float4 r = b.res[slot];
     b.res[slot] = make_float4(r.x + pathSample.x, r.y + pathSample.y, r.z + pathSample.z,
                               __uint_as_float(__float_as_uint(r.w) + 1u));
+    if (a.bilat) reinterpret_cast<float*>(b.dsm + slot)[3] = pot;
     return;
   }
   const uint32_t smp = b.slotSmp[slot];
@@ -439,12 +476,20 @@ __device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a
   Surf sf = load_surf(S, __float_as_uint(h4.y), hw, hu, hv, a.gbuffer && depth == 0);
   Mat m = load_mat(S, sf.mat);
   Bounce B;
-  sample_bounce(orig, dir, h4.x, sf.norm, m, u, a.specPush != 0, B);
+  sample_bounce(orig, dir, h4.x, sf.norm, m, u, a.specPush != 0, a.bilat != 0, a.ptsc != 0, B);
   pathSample = pathSample + vmul(m.emis, outMul);
-  if (a.gbuffer && depth == 0) {  // AdapBilatAtomic.cu:471-476
-    b.gbuf[3 * (size_t)slot] = st4(sf.pos, 0.f);
-    b.gbuf[3 * (size_t)slot + 1] = st4(B.nl, 0.f);
-    b.gbuf[3 * (size_t)slot + 2] = st4(m.diff, 0.f);
+  if (a.gbuffer && depth == 0) {  // AdapBilatAtomic.cu:471-476, Bilat.cu:632-638
+    const bool be = a.bilat != 0;
+    b.gbuf[3 * (size_t)slot] = st4(sf.pos, be ? m.emis.x : 0.f);
+    b.gbuf[3 * (size_t)slot + 1] = st4(B.nl, be ? m.emis.y : 0.f);
+    b.gbuf[3 * (size_t)slot + 2] = st4(m.diff, be ? m.emis.z : 0.f);
+  }
+  if (a.bilat) {  // Bilat.cu:628-631
+    pot = pot * B.pdf;
+    if (depth < 2) {
+      const float4 q = b.dsm[slot];
+      b.dsm[slot] = make_float4(q.x + pathSample.x, q.y + pathSample.y, q.z + pathSample.z, q.w);
+    }
   }
   const f3 inMul = outMul;
   float contrib = length(outMul) * length(B.lmt);
@@ -453,15 +498,16 @@ __device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a
     const float4 r = b.res[slot];
     b.res[slot] = make_float4(r.x + pathSample.x, r.y + pathSample.y, r.z + pathSample.z,
                               __uint_as_float(__float_as_uint(r.w) + 1u));
+    if (a.bilat) reinterpret_cast<float*>(b.dsm + slot)[3] = pot;
     return;
   }
   io.cont = true;
   outMul = vmul(outMul, B.lmt);
   io.o = st4u(B.nOrig, slot);
   io.d = st4u(B.nDir, pix);
-  io.t = st4(outMul, 0.f);
+  io.t = st4(outMul, pot);
   io.s = st4(pathSample, 0.f);
-  if (B.type != kTypeDiff || cacheSize == 0) return;
+  if (B.type != kTypeDiff || cacheSize == 0 || a.ptsc) return;
   // connection: pick a cached light vertex, shade both ends (:665-723)
   f3 pos = B.nOrig + B.nl * kBias;
   uint32_t li = (uint32_t)(u[7] * (float)cacheSize);
@@ -564,8 +610,8 @@ __global__ void __launch_bounds__(kBlock) k_shade(DevScene S, FrameArgs a, Rende
 // applied before the next bounce is shaded), so results are identical.
 enum : uint32_t { kIdle = 0, kPathExt = 1, kPathShadow = 2 };
 
-template <bool kCount>
-__global__ void __launch_bounds__(kBlock) k_tail(DevScene S, FrameArgs a, RenderBuffers b, int in, int shIn,
+template <bool kCount, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_tail(DevScene S, FrameArgs a, RenderBuffers b, int in, int shIn,
                                                  uint32_t depth0, uint32_t kRefill) {
   const uint32_t n = b.ctr->wave[in];
   const uint32_t cacheSize = b.ctr->cacheSize[a.cacheSel];
@@ -621,6 +667,7 @@ __global__ void __launch_bounds__(kBlock) k_tail(DevScene S, FrameArgs a, Render
         const float4 r = b.res[slot];
         b.res[slot] = make_float4(r.x + io.shC.x, r.y + io.shC.y, r.z + io.shC.z,
                                   __uint_as_float(__float_as_uint(r.w) + 4u));
+        if (a.bilat && depth <= 1) direct_connect(b.dsm, slot, io.shC);
       }
       mode = kPathExt;  // the path's next extension ray
       w.init(ld3(io.o), ld3(io.d), gb::kInf, gb::kBias, stack);
@@ -690,6 +737,71 @@ __global__ void k_apply(FrameArgs a, RenderBuffers b, float* result, uint32_t* s
   }
 }
 
+// Filter-only mode (pt_applyPathQueueResult_kernel of
+// src/cudaRTBDPTStreamBilat.cu:989-1051): the running means have no inf test
+// here; direct light and 1 - potential are running means too; the first-hit
+// planes hold this frame's values.
+__global__ void k_apply_bilat(FrameArgs a, RenderBuffers b, float* result, uint32_t* sampleN, float* gpos,
+                              float* gnorm, float* gdiff, float* gemis, float* direct, float* pot) {
+  const uint32_t np = a.width * a.height;
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const float4 r = b.res[p];
+  const uint32_t n = __float_as_uint(r.w);
+  if (n == 0) return;
+  uint32_t old = (a.frame == 0) ? 0u : sampleN[p];
+  if (a.frame == 0) sampleN[p] = 0;
+  const uint32_t nn = old + n;
+  if (!(nn > old)) return;
+  const float rInf = 1.f / (float)nn;
+  const float oInf = (float)old * rInf;
+  const float4 ds = b.dsm[p];
+  float* q = result + 3 * (size_t)p;
+  q[0] = fmaxf(rInf * r.x + oInf * q[0], 0.f);
+  q[1] = fmaxf(rInf * r.y + oInf * q[1], 0.f);
+  q[2] = fmaxf(rInf * r.z + oInf * q[2], 0.f);
+  pot[p] = fmaxf(rInf * (1.f - ds.w) + oInf * pot[p], 0.f);
+  sampleN[p] = nn;
+  float* dq = direct + 3 * (size_t)p;
+  dq[0] = rInf * ds.x + oInf * dq[0];
+  dq[1] = rInf * ds.y + oInf * dq[1];
+  dq[2] = rInf * ds.z + oInf * dq[2];
+  const float4 g0 = b.gbuf[3 * (size_t)p], g1 = b.gbuf[3 * (size_t)p + 1], g2 = b.gbuf[3 * (size_t)p + 2];
+  const size_t o = 3 * (size_t)p;
+  gpos[o] = g0.x, gpos[o + 1] = g0.y, gpos[o + 2] = g0.z;
+  gnorm[o] = g1.x, gnorm[o + 1] = g1.y, gnorm[o + 2] = g1.z;
+  gemis[o] = g0.w, gemis[o + 1] = g1.w, gemis[o + 2] = g2.w;
+  gdiff[o] = g2.x, gdiff[o + 1] = g2.y, gdiff[o + 2] = g2.z;
+}
+
+// Unidirectional mode: one path per pixel, weights of the frame index.
+__global__ void k_apply_pt(FrameArgs a, RenderBuffers b, float* result, uint32_t* sampleN) {
+  using namespace gb;
+  const uint32_t np = a.width * a.height;
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const float4 r = b.res[p];
+  const uint32_t n = __float_as_uint(r.w);
+  if (n == 0) return;
+  const f3 smp = ld3(r) / (float)n;
+  const float rInf = 1.f / (float)(a.frame + 1);
+  const float oInf = 1.f - rInf;
+  float* q = result + 3 * (size_t)p;
+  q[0] = fmaxf(rInf * smp.x + oInf * q[0], 0.f);
+  q[1] = fmaxf(rInf * smp.y + oInf * q[1], 0.f);
+  q[2] = fmaxf(rInf * smp.z + oInf * q[2], 0.f);
+  sampleN[p] = a.frame + 1;  // frames so far (the reference keeps no count in this mode)
+}
+
+__global__ void k_prob_view(const float* pot, uint32_t np, float minProb, float* out) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const float v = fmaxf(minProb, pot[p]);
+  out[3 * (size_t)p] = v;
+  out[3 * (size_t)p + 1] = v;
+  out[3 * (size_t)p + 2] = v;
+}
+
 // ---------------------------------------------------------------------------
 // Stand-alone TracePrimitive for caller-supplied rays.
 template <bool kCount>
@@ -737,6 +849,10 @@ uint32_t grid_for(const void* kernel) {
 
 }  // namespace
 
+static std::atomic<uint64_t> g_launches{0};
+void note_launches(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
 int sm_count() {
   if (!g_sm) {
     int dev = 0;
@@ -751,36 +867,79 @@ cudaError_t launch_light_pass(const DevScene& S, const FrameArgs& a, const Rende
   uint32_t threads = ((a.lightPaths + 31) / 32) * 32;
   if (threads == 0) threads = 32;
   k_light<<<1, threads, 0, st>>>(S, a, b.cache[a.cacheSel], b.cacheCap, b.ctr);
+  note_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream_t st) {
   const uint32_t np = a.width * a.height;
   k_camera<<<(np + kBlock - 1) / kBlock, kBlock, 0, st>>>(a, b);
+  note_launches(1);
   return cudaGetLastError();
 }
 
+// Resident CTAs per SM the walk kernels are compiled for (register caps
+// 64 / 48 / 40 for k_walk, 128 / 80 for k_tail); GBPT_WALK_MINB /
+// GBPT_TAIL_MINB select a variant (tuning knobs; defaults from measurement).
+int walk_minb() {
+  static int v = [] {
+    const char* e = std::getenv("GBPT_WALK_MINB");
+    int x = e ? std::atoi(e) : 4;
+    return x >= 6 ? 6 : x == 5 ? 5 : 4;
+  }();
+  return v;
+}
+int tail_minb() {
+  static int v = [] {
+    const char* e = std::getenv("GBPT_TAIL_MINB");
+    int x = e ? std::atoi(e) : 2;
+    return x >= 3 ? 3 : 2;
+  }();
+  return v;
+}
+
+template <bool kCount, int kMinB>
+void walk_variant(const DevScene& S, const RenderBuffers& b, int in, int shIn, int shReset, uint32_t sd,
+                  cudaStream_t st) {
+  static uint32_t g = grid_for((const void*)k_walk<kCount, kMinB>);
+  k_walk<kCount, kMinB><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, sd, walk_refill());
+}
+
+template <bool kCount, int kMinB>
+void tail_variant(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn, uint32_t depth0,
+                  cudaStream_t st) {
+  static uint32_t g = grid_for((const void*)k_tail<kCount, kMinB>);
+  k_tail<kCount, kMinB><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill());
+}
+
 cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
-                        int shReset, cudaStream_t st) {
+                        int shReset, bool shDirect, cudaStream_t st) {
+  const uint32_t sd = (a.bilat && shDirect) ? 1u : 0u;
+  const int mb = walk_minb();
   if (a.counting) {
-    static uint32_t g = grid_for((const void*)k_walk<true>);
-    k_walk<true><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, walk_refill());
+    if (mb == 6) walk_variant<true, 6>(S, b, in, shIn, shReset, sd, st);
+    else if (mb == 5) walk_variant<true, 5>(S, b, in, shIn, shReset, sd, st);
+    else walk_variant<true, 4>(S, b, in, shIn, shReset, sd, st);
   } else {
-    static uint32_t g = grid_for((const void*)k_walk<false>);
-    k_walk<false><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, walk_refill());
+    if (mb == 6) walk_variant<false, 6>(S, b, in, shIn, shReset, sd, st);
+    else if (mb == 5) walk_variant<false, 5>(S, b, in, shIn, shReset, sd, st);
+    else walk_variant<false, 4>(S, b, in, shIn, shReset, sd, st);
   }
+  note_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
                         uint32_t depth0, cudaStream_t st) {
+  const int mb = tail_minb();
   if (a.counting) {
-    static uint32_t g = grid_for((const void*)k_tail<true>);
-    k_tail<true><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill());
+    if (mb == 3) tail_variant<true, 3>(S, a, b, in, shIn, depth0, st);
+    else tail_variant<true, 2>(S, a, b, in, shIn, depth0, st);
   } else {
-    static uint32_t g = grid_for((const void*)k_tail<false>);
-    k_tail<false><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill());
+    if (mb == 3) tail_variant<false, 3>(S, a, b, in, shIn, depth0, st);
+    else tail_variant<false, 2>(S, a, b, in, shIn, depth0, st);
   }
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -801,6 +960,7 @@ cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuff
                          bool attach, cudaStream_t st) {
   static uint32_t g = grid_for((const void*)k_shade);
   k_shade<<<g, kBlock, 0, st>>>(S, a, b, in, depth, attach ? 1u : 0u);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -808,6 +968,32 @@ cudaError_t launch_apply(const FrameArgs& a, const RenderBuffers& b, float* resu
                          float* gnorm, float* gdiff, cudaStream_t st) {
   const uint32_t np = a.width * a.height;
   k_apply<<<(np + kBlock - 1) / kBlock, kBlock, 0, st>>>(a, b, result, sampleN, gpos, gnorm, gdiff);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_apply_bilat(const FrameArgs& a, const RenderBuffers& b, float* result, uint32_t* sampleN,
+                               float* gpos, float* gnorm, float* gdiff, float* gemis, float* direct, float* pot,
+                               cudaStream_t st) {
+  const uint32_t np = a.width * a.height;
+  k_apply_bilat<<<(np + kBlock - 1) / kBlock, kBlock, 0, st>>>(a, b, result, sampleN, gpos, gnorm, gdiff, gemis,
+                                                               direct, pot);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_apply_pt(const FrameArgs& a, const RenderBuffers& b, float* result, uint32_t* sampleN,
+                            cudaStream_t st) {
+  const uint32_t np = a.width * a.height;
+  k_apply_pt<<<(np + kBlock - 1) / kBlock, kBlock, 0, st>>>(a, b, result, sampleN);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prob_view(const float* pot, uint32_t np, float minProb, float* out, cudaStream_t st) {
+  if (np == 0) return cudaSuccess;
+  k_prob_view<<<(np + kBlock - 1) / kBlock, kBlock, 0, st>>>(pot, np, minProb, out);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -822,6 +1008,7 @@ cudaError_t launch_trace_rays(const DevScene& S, const float* rays, uint32_t n, 
   else
     k_trace_rays<false><<<grid, kBlock, 0, st>>>(S, rays, n, maxDist, eps, cullback, t, tri, w, u, v, nodes,
                                                    trisTested);
+  note_launches(1);
   return cudaGetLastError();
 }
 

@@ -58,6 +58,8 @@ struct FrameArgs {
   uint32_t counting;    // node/triangle counters
   uint32_t useEnv;      // env != 0: add env * throughput on a miss
   uint32_t cacheSel;    // light-vertex cache (0/1) this frame reads or the light pass writes
+  uint32_t bilat;       // filter-only mode: direct-light sample, path potential, first-hit emissive
+  uint32_t ptsc;        // unidirectional mode: no connections, total internal reflection reflects
 };
 
 struct RenderBuffers {
@@ -66,7 +68,9 @@ struct RenderBuffers {
   float4* sh[2];        // connection queues (bounce parity), 3 float4 per entry:
                         // {origin, slot} {dir, maxDist} {weighted contribution}
   float4* res;          // per slot: acc.xyz, n bits
-  float4* gbuf;         // per slot: 3 float4 (pos, normal, diffuse) when gbuffer
+  float4* gbuf;         // per slot: 3 float4 (pos, normal, diffuse) when gbuffer; with bilat the
+                        // three .w words hold the first-hit emissive
+  float4* dsm;          // bilat, per slot: direct-light sample .xyz, path potential at termination .w
   uint32_t* slotPix;    // per slot pixel id
   uint32_t* slotSmp;    // per slot sample id
   float4* cache[2];     // two light-vertex caches (6 float4 per vertex): one is read by the
@@ -82,8 +86,10 @@ cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream
 // one persistent walk over the extension rays of wave `in` (in < 0: none)
 // followed by the shadow rays of connection queue `shIn` (shIn < 0: none);
 // resets the counters of wave in^1 and of connection queue `shReset`
+// (shDirect: the connection queue holds bounce-0 connections, which update
+// the direct-light sample of the filter-only mode)
 cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
-                        int shReset, cudaStream_t st);
+                        int shReset, bool shDirect, cudaStream_t st);
 // attach: store each continuing path's connection at the path's index (for the tail kernel)
 cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t depth,
                          bool attach, cudaStream_t st);
@@ -95,6 +101,18 @@ cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffe
 uint32_t tail_from(uint32_t eyeDepth);
 cudaError_t launch_apply(const FrameArgs& a, const RenderBuffers& b, float* result, uint32_t* sampleN, float* gpos,
                          float* gnorm, float* gdiff, cudaStream_t st);
+// filter-only mode (src/cudaRTBDPTStreamBilat.cu:989-1051): running means of
+// the result (no inf filter), the direct-light sample and 1 - path potential;
+// the first-hit planes are overwritten with this frame's values
+cudaError_t launch_apply_bilat(const FrameArgs& a, const RenderBuffers& b, float* result, uint32_t* sampleN,
+                               float* gpos, float* gnorm, float* gdiff, float* gemis, float* direct, float* pot,
+                               cudaStream_t st);
+// unidirectional mode (pt_applyPathQueueResult_kernel of src/cudaRTPTStream.cu:335-358):
+// result = max(acc/n / (frame+1) + (1 - 1/(frame+1)) * result, 0)
+cudaError_t launch_apply_pt(const FrameArgs& a, const RenderBuffers& b, float* result, uint32_t* sampleN,
+                            cudaStream_t st);
+// "Prob" debug views (pt_applyPixelProbToResult_kernel, :933-940): RGB = max(minProb, pot)
+cudaError_t launch_prob_view(const float* pot, uint32_t np, float minProb, float* out, cudaStream_t st);
 cudaError_t launch_trace_rays(const DevScene& S, const float* rays, uint32_t n, float maxDist, float eps, int cullback,
                               float* t, int32_t* tri, float* w, float* u, float* v, uint32_t* nodes,
                               uint32_t* trisTested, cudaStream_t st);
@@ -131,5 +149,8 @@ cudaError_t launch_fmath(int which, const float* x, uint32_t n, float* out, cuda
 cudaError_t launch_philox(const uint32_t* ctr, uint32_t n, uint32_t k0, uint32_t k1, uint32_t* out, cudaStream_t st);
 
 int sm_count();
+// Kernels this library has launched so far (every launcher adds its count).
+void note_launches(uint32_t n);
+uint64_t launch_count();
 
 }  // namespace gbpt

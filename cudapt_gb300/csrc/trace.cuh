@@ -174,8 +174,8 @@ struct Walk {
     const uint32_t off = __float_as_uint(a.w);
     const uint32_t tn = __float_as_uint(b.w);
     if (tn == 0) {
-      if (sp < 29) {  // push cur+1 then cur+off (the reference's order); top stays in tos
-        if (sp >= 0) stack[sp] = tos;
+      if (sp < 29) {  // push cur+1 then cur+off (the reference's order); cur+off becomes tos
+        // (stack[sp] already holds the current tos: it was just reloaded from there)
         stack[sp + 1] = cur + 1;
         sp += 2;
         tos = cur + off;

@@ -56,6 +56,15 @@ PARAMS = np.dtype(
         ("filter_sigma_spatial", "<f4"),
         ("request_id", "<u4"),
         ("min_trace_prob", "<f4"),
+        ("bilat_color_eud", "<f4"),
+        ("bilat_pos_eud", "<f4"),
+        ("bilat_norm_eud", "<f4"),
+        ("bilat_emit_eud", "<f4"),
+        ("bilat_diff_eud", "<f4"),
+        ("bilat_radius", "<u4"),
+        ("filter_iterations", "<u4"),
+        ("render_iterations", "<u4"),
+        ("pt_depth_max", "<u4"),
     ]
 )
 
@@ -64,12 +73,20 @@ PARAMS = np.dtype(
 MODE_BDPT_SC = 0              # "BDPTSC"                     cudaRTBDPTStream
 MODE_BDPT_SC_ADAP_BILAT = 1   # "BDPTSC Adap Bilat PLL"      cudaRTBDPTStreamAdapBilatAtomic
 MODE_BDPT_SC_ADAP_BILAT_BINARY = 2  # "BDPTSC Adap Bilat Binary"  cudaRTBDPTStreamAdapBilatBinary
+MODE_BDPT_SC_BILAT = 3        # "BDPTSC Bilaterial"          cudaRTBDPTStreamBilat
+MODE_PT_SC = 4                # "PTSC" (unidirectional)      cudaRTPTStream
+
+# gbpt_read_buffer ids
+BUF_RESULT, BUF_POS, BUF_NORM, BUF_DIFF, BUF_FILTERED, BUF_ERR, BUF_SAMPLE_N, BUF_LIGHT_CACHE = range(8)
+BUF_DIRECT, BUF_EMIS, BUF_POTENTIAL = 8, 9, 10
 
 
 def default_params(**over):
     """Reference defaults: depth caps 5/5 (src/cudaRTBDPTStream.cu:7,10),
     128 light paths every 3rd frame (:875-877), adaptive knobs of
-    src/cudaRTBDPTStreamAdapBilatAtomic.cu:26-37, warm-up 5 frames (:1372)."""
+    src/cudaRTBDPTStreamAdapBilatAtomic.cu:26-37, warm-up 5 frames (:1372),
+    filter-only knobs of src/cudaRTBDPTStreamBilat.cu:29-37, PTSC depth cap 10
+    (src/cudaRTPTStream.cu:6)."""
     p = np.zeros((), PARAMS)
     p["seed"] = 1234
     p["eye_depth_max"] = 5
@@ -88,6 +105,15 @@ def default_params(**over):
     p["filter_sigma_spatial"] = 0.0
     p["request_id"] = 0
     p["min_trace_prob"] = 0.0
+    p["bilat_color_eud"] = 1.0
+    p["bilat_pos_eud"] = 1.0
+    p["bilat_norm_eud"] = 1.0
+    p["bilat_emit_eud"] = 0.5
+    p["bilat_diff_eud"] = 0.5
+    p["bilat_radius"] = 5
+    p["filter_iterations"] = 1
+    p["render_iterations"] = 5
+    p["pt_depth_max"] = 10
     for k, v in over.items():
         p[k] = v
     return p

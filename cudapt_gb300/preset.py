@@ -23,16 +23,18 @@ import re
 
 import numpy as np
 
-from .layouts import MATERIAL, MODE_BDPT_SC, MODE_BDPT_SC_ADAP_BILAT, MODE_BDPT_SC_ADAP_BILAT_BINARY
+from .layouts import (MATERIAL, MODE_BDPT_SC, MODE_BDPT_SC_ADAP_BILAT, MODE_BDPT_SC_ADAP_BILAT_BINARY,
+                      MODE_BDPT_SC_BILAT, MODE_PT_SC)
 
 # RTRenderer::RENDERER_MODE with FULLSPECTRAL off (include/raytracer.h:1-26,
 # 295-304): CPU debug, then the X-macro entries in order.
 RTTECH_NAMES = ["CPU Debug", "RasterizeBasic", "PTNaive", "PTSC", "BDPTRegen", "BDPTSC", "BDPTSC Bilaterial",
                 "BDPTSC Adap Bilat Binary", "BDPTSC Adap Bilat PLL", "BDPTSA Adap Bilat PLL", "Cuda Debug",
                 "Cuda BVH Debug"]
-RTTECH_TO_MODE = {5: MODE_BDPT_SC, 7: MODE_BDPT_SC_ADAP_BILAT_BINARY, 8: MODE_BDPT_SC_ADAP_BILAT,
-                  9: MODE_BDPT_SC_ADAP_BILAT}
-MODE_TO_RTTECH = {MODE_BDPT_SC: 5, MODE_BDPT_SC_ADAP_BILAT_BINARY: 7, MODE_BDPT_SC_ADAP_BILAT: 8}
+RTTECH_TO_MODE = {3: MODE_PT_SC, 5: MODE_BDPT_SC, 6: MODE_BDPT_SC_BILAT, 7: MODE_BDPT_SC_ADAP_BILAT_BINARY,
+                  8: MODE_BDPT_SC_ADAP_BILAT, 9: MODE_BDPT_SC_ADAP_BILAT}
+MODE_TO_RTTECH = {MODE_PT_SC: 3, MODE_BDPT_SC: 5, MODE_BDPT_SC_BILAT: 6, MODE_BDPT_SC_ADAP_BILAT_BINARY: 7,
+                  MODE_BDPT_SC_ADAP_BILAT: 8}
 
 _MAT_FIELDS = [("anisotropic", 1), ("clearcoat", 1), ("clearcoatGloss", 1), ("diffuse", 3), ("diffuseTexId", 1),
                ("emissive", 3), ("emissiveTexId", 1), ("metallic", 1), ("normalTexId", 1), ("roughness", 1),

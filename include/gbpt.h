@@ -82,6 +82,17 @@ typedef struct gbpt_params {
                                  reference's table built from the colour delta */
   uint32_t request_id;      /* Philox key word 1 (0) */
   float min_trace_prob;     /* "Min Trace Probability" of the binary allocator (0) */
+  /* "BDPTSC Bilaterial" (filter-only mode, src/cudaRTBDPTStreamBilat.cu:26-52):
+   * its own filter deltas, pass counts and frame limit */
+  float bilat_color_eud;    /* "Filter Color E Delta" (1) */
+  float bilat_pos_eud;      /* "Filter Pos E Delta" (1) */
+  float bilat_norm_eud;     /* "Filter Norm E Delta" (1) */
+  float bilat_emit_eud;     /* "Filter Emit E Delta" (0.5; kept, the reference's filter call does not read it) */
+  float bilat_diff_eud;     /* "Filter Diff E Delta" (0.5): the first-hit diffuse plane's delta */
+  uint32_t bilat_radius;    /* "Filter Radius" (5, <= 31) */
+  uint32_t filter_iterations; /* "Filter Iteration" (1): filter passes per frame, ping-pong */
+  uint32_t render_iterations; /* "Render Iteration" (5): frames that trace paths; 0 = no limit */
+  uint32_t pt_depth_max;    /* "PTSC" bounce cap, NORMALRAY_BOUND_MAX of src/cudaRTPTStream.cu:6 (10) */
 } gbpt_params;
 
 /* Renderer modes: the BDPT entries of the X-macro registry
@@ -89,7 +100,9 @@ typedef struct gbpt_params {
 typedef enum gbpt_mode {
   GBPT_MODE_BDPT_SC = 0,                  /* "BDPTSC"                    cudaRTBDPTStream */
   GBPT_MODE_BDPT_SC_ADAP_BILAT = 1,       /* "BDPTSC Adap Bilat PLL"     cudaRTBDPTStreamAdapBilatAtomic */
-  GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY = 2 /* "BDPTSC Adap Bilat Binary"  cudaRTBDPTStreamAdapBilatBinary */
+  GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY = 2, /* "BDPTSC Adap Bilat Binary"  cudaRTBDPTStreamAdapBilatBinary */
+  GBPT_MODE_BDPT_SC_BILAT = 3,            /* "BDPTSC Bilaterial"          cudaRTBDPTStreamBilat */
+  GBPT_MODE_PT_SC = 4                     /* "PTSC" (unidirectional)     cudaRTPTStream */
 } gbpt_mode;
 
 /* Per-frame statistics (the reference's PERFBREAKDOWN timers,
@@ -111,6 +124,7 @@ typedef struct gbpt_stats {
   float ms_shadow;         /* 0: shadow rays are walked together with the next bounce's rays */
   float ms_filter;         /* bilateral filter */
   float ms_adapt;          /* error, budget and accumulation kernels */
+  uint32_t launches;       /* kernels this library launched during the call (all streams) */
 } gbpt_stats;
 
 typedef struct gbpt_scene gbpt_scene;
@@ -176,8 +190,12 @@ gbpt_status gbpt_render_frames(gbpt_renderer* r, gbpt_scene* s, const gbpt_camer
  * the last result (refreshed by gbpt_render / gbpt_read_result). */
 const float* gbpt_result(gbpt_renderer* r);
 /* Copies a renderer buffer: 0 result RGB, 1 first-hit position, 2 normal,
- * 3 diffuse (G-buffer of the adaptive mode), 4 filtered RGB, 5 per-pixel error
- * (W*H floats), 6 per-pixel sample count (W*H uint32). */
+ * 3 diffuse (G-buffer: count-weighted means in the adaptive modes, the last
+ * frame's first hit in BDPT_SC_BILAT), 4 filtered RGB, 5 per-pixel error
+ * (W*H floats), 6 per-pixel sample count (W*H uint32), 7 light-vertex cache
+ * (21 floats per vertex), and in BDPT_SC_BILAT: 8 direct-light running mean
+ * RGB, 9 first-hit emissive RGB, 10 running mean of 1 - path potential
+ * (W*H floats; the "Prob" debug view). */
 gbpt_status gbpt_read_buffer(gbpt_renderer* r, int32_t which, void* dst, size_t bytes, int32_t dst_is_device);
 /* Restart progressive accumulation (next frame is frame 0). */
 gbpt_status gbpt_reset(gbpt_renderer* r);
@@ -187,7 +205,15 @@ gbpt_status gbpt_clean(gbpt_renderer* r);
 /* Enable per-frame node/triangle counters (costs one atomic per warp and step). */
 gbpt_status gbpt_set_counting(gbpt_renderer* r, int32_t on);
 
-/* ---- attributes: GetAttribute / GetAttribsN (src/raytracer.cpp:19-31) ----- */
+/* ---- attributes: GetAttribute / GetAttribsN (src/raytracer.cpp:19-31) -----
+ * The names are the current mode's: the adaptive modes list the reference's
+ * "Desired Max Sampling", "Filter Color EuD", ... (AdapBilatAtomic.cu:48-60);
+ * BDPT_SC_BILAT lists "Filter Color E Delta" ... "Render Iteration"
+ * (src/cudaRTBDPTStreamBilat.cu:40-50).  Both add the knobs the reference kept
+ * as defines (depth caps, light paths, seed).  "Debug Mode" selects the view
+ * gbpt_render copies out: adaptive modes 0 result, 4 filtered; BDPT_SC_BILAT
+ * 0/1 filtered, 2/3 filtered path-potential view, 4 direct light, 5 position,
+ * 6 normal, 7 unfiltered result. */
 gbpt_status gbpt_attr_count(const gbpt_renderer* r, uint32_t* n);
 gbpt_status gbpt_attr_name(const gbpt_renderer* r, uint32_t index, char* name, size_t cap);
 gbpt_status gbpt_attr_get(const gbpt_renderer* r, const char* name, float* value);
@@ -216,6 +242,23 @@ gbpt_status gbpt_bilateral(const float* color, const float* pos, const float* no
 gbpt_status gbpt_bilateral_noalloc(const float* color, const float* pos, const float* norm, const float* emit,
                                    uint32_t width, uint32_t height, float color_eud, float pos_eud, float norm_eud,
                                    float emit_eud, uint32_t radius, const float* g, float* out, void* stream);
+
+/* ---- RMSE experiments and image export (src/cudapt.cpp:482-619, 867-997) ---
+ * RMSE = sqrt(sum((a - b)^2) / n) over n floats, summed in double on the
+ * device (the reference sums in float on the host). */
+gbpt_status gbpt_rmse(const float* a, const float* b, uint64_t n, int32_t is_device, double* out);
+/* RMSE of the image gbpt_render would copy out (the current view) against a
+ * converged W*H*3 image (CUDAPTWindow::CalculateRMSE), without copying the
+ * view to the host. */
+gbpt_status gbpt_renderer_rmse(gbpt_renderer* r, const float* converged, int32_t converged_is_device, double* out);
+/* 8-bit RGBA export, top row first (the float image has row 0 at the bottom):
+ * kind 0 the tone-mapped result of BrowseAndSaveResult (clamp to [0,1],
+ * 1 - exp(-x * exposure), x^(1/2.2)); kind 1 the per-pixel MSE against ref of
+ * BrowseAndSaveMSEResult; kind 2 clamp to [0,1] (ExportConvergedResult).
+ * bytes = (unsigned char)(x * 255); alpha 255.  Device arrays (is_device) must
+ * be 4-byte aligned. */
+gbpt_status gbpt_tonemap_rgba8(const float* rgb, const float* ref, uint32_t width, uint32_t height, float exposure,
+                               int32_t kind, uint8_t* out_rgba, int32_t is_device);
 
 /* ---- device math, exposed for verification -------------------------------
  * Evaluated by a kernel on host arrays x/out (copied in and out).

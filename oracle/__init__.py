@@ -62,9 +62,11 @@ def lib():
             L.orc_render.argtypes = [vp, vp, vp, u32]
             L.orc_renderer_get.argtypes = [vp, i32, vp]
             L.orc_renderer_counts.argtypes = [vp, vp, vp]
+            L.orc_renderer_set_debug.argtypes = [vp, u32]
             L.orc_renderer_frame.restype = u32
             L.orc_renderer_frame.argtypes = [vp]
             L.orc_renderer_stats.argtypes = [vp, vp]
+            L.orc_renderer_ext_stats.argtypes = [vp, vp]
             L.orc_renderer_light_cache.restype = u32
             L.orc_renderer_light_cache.argtypes = [vp, vp]
             L.orc_render_fp64.argtypes = [vp, vp, u32, u32, vp, u32, u32, vp]
@@ -161,8 +163,14 @@ class Renderer:
         c = cam_array(cam)
         lib().orc_render(self.h, scene.h, _p(c), frames)
 
+    def set_debug(self, mode):
+        """Debug view of the filter-only mode (0..7)."""
+        lib().orc_renderer_set_debug(self.h, mode)
+
     def get(self, which=0):
-        n = self.W * self.H * (1 if which == 5 else 3)
+        """0 result, 1 position, 2 normal, 3 diffuse, 4 filtered, 5 error; filter-only
+        mode: 8 direct, 9 first-hit emissive, 10 mean 1 - potential, 11 the debug view."""
+        n = self.W * self.H * (1 if which in (5, 10) else 3)
         out = np.zeros(n, np.float32)
         lib().orc_renderer_get(self.h, which, _p(out))
         return out
@@ -180,7 +188,10 @@ class Renderer:
     def stats(self):
         s = np.zeros(4, np.uint64)
         lib().orc_renderer_stats(self.h, _p(s))
-        return dict(paths=int(s[0]), rays=int(s[1]), nodes=int(s[2]), tris=int(s[3]))
+        e = np.zeros(3, np.uint64)
+        lib().orc_renderer_ext_stats(self.h, _p(e))
+        return dict(paths=int(s[0]), rays=int(s[1]), nodes=int(s[2]), tris=int(s[3]), ext_rays=int(e[0]),
+                    ext_nodes=int(e[1]), ext_tris=int(e[2]))
 
     def light_cache(self):
         n = lib().orc_renderer_light_cache(self.h, None)

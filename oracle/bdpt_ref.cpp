@@ -365,23 +365,39 @@ static bool traceR(const Scene& s, V<double> o, V<double> d, double maxDist, Hit
 
 // ---- eye path: pt_traceSample_kernel loop + connections ---------------------
 template <typename R>
+//
+// bilat: the filter-only variant's extra per-path outputs
+// (src/cudaRTBDPTStreamBilat.cu:472-671, :884-915): the sampling density
+// product ("path potential", :515-518 and per branch :560/:575/:599, :627),
+// the direct-light sample (pathSample added at bounces 0 and 1, :628-631; the
+// bounce-0 connection's light L turns it into (direct + L)/5, or L/4 when no
+// channel is positive, :907-913) and the first-hit emissive (:636).
+//
+// pt: the unidirectional "PTSC" path of src/cudaRTPTStream.cu:91-258 -- no
+// connections, total internal reflection reflects (cos2t < 0 sets reflProb =
+// 1, :153-160), depth cap pt_depth_max.
 static void eye_path(const Scene& s, const Params& p, const LightVertex* cache, uint32_t cacheSize, V<R> orig,
-                     V<R> dir, uint32_t pathId, uint32_t frame, uint32_t sample, bool specPush, PathResult* out) {
+                     V<R> dir, uint32_t pathId, uint32_t frame, uint32_t sample, bool specPush, bool bilat,
+                     bool pt, PathResult* out) {
   V<R> outMul = mkv<R>(1, 1, 1), pathSample = mkv<R>(0, 0, 0), acc = mkv<R>(0, 0, 0);
+  V<R> direct = mkv<R>(0, 0, 0);
+  R pot = (R)1;
   uint32_t n = 0, depth = 0;
-  TraceCount cnt;
-  uint32_t rays = 0;
-  for (int k = 0; k < 3; k++) out->gpos[k] = out->gnorm[k] = out->gdiff[k] = 0;
+  TraceCount cnt, cntS;  // extension walks, connection (shadow) walks
+  uint32_t rays = 0, extRays = 0;
+  for (int k = 0; k < 3; k++) out->gpos[k] = out->gnorm[k] = out->gdiff[k] = out->gemis[k] = 0;
   const R bias = K<R>::bias;
   while (true) {
     HitR<R> hit;
     rays++;
+    extRays++;
     if (!traceR(s, orig, dir, K<R>::inf, &hit, false, &cnt)) {
       // miss: optional constant environment, then accumulate and stop
       if (p.env[0] != 0.f || p.env[1] != 0.f || p.env[2] != 0.f)
         pathSample = pathSample + vmulv(mkv<R>((R)p.env[0], (R)p.env[1], (R)p.env[2]), outMul);
       acc = acc + pathSample;
       n++;
+      out->pot = (double)pot;
       break;
     }
     float u[8];
@@ -397,6 +413,11 @@ static void eye_path(const Scene& s, const Params& p, const LightVertex* cache, 
     R voH = dotv(ndir, hDir);
     V<R> f0 = lerpv(K<R>::f0s * mkv<R>(specular, specular, specular), diff, metallic);
     V<R> F = f_schlick(f0, voH);
+    R pdf = (R)1;
+    if (bilat) {
+      R NoH0 = dotv(nl, hDir);
+      pdf = (d_ggx(rough, NoH0) * NoH0) / ((R)4 * voH);
+    }
     R reflProb = lerpR(lenR(F), (R)1, metallic);
     R refrProb = trans;
     V<R> reflDir = mkv<R>(0, 0, 0), refrDir = mkv<R>(0, 0, 0);
@@ -407,7 +428,10 @@ static void eye_path(const Scene& s, const Params& p, const LightVertex* cache, 
       R nnt = into ? nc / nt : nt / nc;
       R ddn = dotv(hDir, dir);
       R cos2t = (R)1 - (nnt * nnt) * ((R)1 - ddn * ddn);
-      refrDir = normv(dir * nnt - hDir * (ddn * nnt + std::sqrt(cos2t)));
+      if (pt && cos2t < (R)0)
+        reflProb = (R)1;
+      else
+        refrDir = normv(dir * nnt - hDir * (ddn * nnt + std::sqrt(cos2t)));
     }
     if (reflProb > (R)0) {
       reflDir = normv(dir - (hDir * (R)2) * dotv(hDir, dir));
@@ -426,18 +450,21 @@ static void eye_path(const Scene& s, const Params& p, const LightVertex* cache, 
       R G = vis_smith(rough, NoV, NoL);
       lmt = ((F * G) * VoH) / ((NoV * NoH) * reflProb);
       nType = kSpec;
+      pdf = pdf * reflProb;
     } else if (prob_rand(refrProb, u[3])) {
       nOrig = (orig + (hit.dist + bias) * dir) + refrDir * bias;
       nDir = refrDir;
       R cosine = dotv((R)-1 * nl, refrDir);
       lmt = (cosine * diff) / (refrProb * ((R)1 - reflProb));
       nType = kSpec;
+      pdf = pdf * (refrProb * ((R)1 - reflProb));
     } else {
       V<R> dd = cos_dir<R>((R)u[4], (R)u[5], nl);
       nOrig = (orig + hit.dist * dir) + dd * bias;
       nDir = dd;
       lmt = (K<R>::pi * (diff * K<R>::inv_pi)) / (((R)1 - refrProb) * ((R)1 - reflProb));
       nType = kDiff;
+      pdf = pdf * ((((R)1 - refrProb) * ((R)1 - reflProb)) * dotv(dd, nl));
     }
     pathSample = pathSample + vmulv(emissive, outMul);
     if (depth == 0) {  // G-buffer, AdapBilatAtomic.cu:471-476
@@ -450,20 +477,28 @@ static void eye_path(const Scene& s, const Params& p, const LightVertex* cache, 
       out->gdiff[0] = (double)diff.x;
       out->gdiff[1] = (double)diff.y;
       out->gdiff[2] = (double)diff.z;
+      out->gemis[0] = (double)emissive.x;
+      out->gemis[1] = (double)emissive.y;
+      out->gemis[2] = (double)emissive.z;
+    }
+    if (bilat) {
+      pot = pot * pdf;
+      if (depth < 2) direct = direct + pathSample;
     }
     V<R> inMul = outMul;
     R contrib = lenR(outMul) * lenR(lmt);
     if (lenR(emissive) > (R)0) contrib = (R)0;
-    if ((R)u[6] > contrib || depth + 1 >= p.eye_depth_max) {
+    if ((R)u[6] > contrib || depth + 1 >= (pt ? p.pt_depth_max : p.eye_depth_max)) {
       acc = acc + pathSample;
       n++;
+      out->pot = (double)pot;
       break;
     }
     outMul = vmulv(outMul, lmt);
     dir = nDir;
     depth++;
     orig = nOrig;
-    if (nType != kDiff) continue;
+    if (nType != kDiff || pt) continue;
     // ---- connection to a cached light vertex (:665-723) ----
     if (cacheSize == 0) continue;
     V<R> pos = orig + nl * bias;
@@ -477,7 +512,7 @@ static void eye_path(const Scene& s, const Params& p, const LightVertex* cache, 
     if (lenR(ld<R>(lv.irrad)) > (R)0 && dotv(nl, toDir) > (R)0) {
       HitR<R> sh;
       rays++;
-      if (!traceR(s, pos, toDir, toDist - bias, &sh, true, &cnt)) {
+      if (!traceR(s, pos, toDir, toDist - bias, &sh, true, &cntS)) {
         if (toDist > K<R>::fltEps) {
           irrad = shading<R>((R)-1 * toDir, ld<R>(lv.irradDir), ld<R>(lv.irrad), ld<R>(lv.norm), ld<R>(lv.diff),
                              (R)lv.metallic, (R)lv.roughness, (R)lv.specular, (R)1, (R)1) +
@@ -494,15 +529,25 @@ static void eye_path(const Scene& s, const Params& p, const LightVertex* cache, 
     if (lenR(c) > (R)0) {
       acc = acc + vmulv(c, inMul);
       n += 4;
+      if (bilat && depth <= 1) {
+        V<R> L = vmulv(c, inMul);
+        direct = (direct.x > (R)0 || direct.y > (R)0 || direct.z > (R)0) ? (direct + L) / (R)5 : L / (R)4;
+      }
     }
   }
+  out->direct[0] = (double)direct.x;
+  out->direct[1] = (double)direct.y;
+  out->direct[2] = (double)direct.z;
   out->acc[0] = (double)acc.x;
   out->acc[1] = (double)acc.y;
   out->acc[2] = (double)acc.z;
   out->n = n;
   out->rays = rays;
-  out->nodes = cnt.nodes;
-  out->tris = cnt.tris;
+  out->nodes = cnt.nodes + cntS.nodes;
+  out->tris = cnt.tris + cntS.tris;
+  out->extRays = extRays;
+  out->extNodes = cnt.nodes;
+  out->extTris = cnt.tris;
 }
 
 // ---- light pass: pt_genLightPathQueue_kernel + pt_traceLight_kernel --------
@@ -734,6 +779,15 @@ void default_params(Params* p) {
   p->filter_sigma_spatial = 0.f;
   p->request_id = 0;
   p->min_trace_prob = 0.f;
+  p->bilat_color_eud = 1.f;
+  p->bilat_pos_eud = 1.f;
+  p->bilat_norm_eud = 1.f;
+  p->bilat_emit_eud = 0.5f;
+  p->bilat_diff_eud = 0.5f;
+  p->bilat_radius = 5;
+  p->filter_iterations = 1;
+  p->render_iterations = 5;
+  p->pt_depth_max = 10;
 }
 
 void renderer_init(Renderer* r, uint32_t W, uint32_t H, int32_t mode, const Params& p, bool fp64, uint32_t threads) {
@@ -752,6 +806,10 @@ void renderer_init(Renderer* r, uint32_t W, uint32_t H, int32_t mode, const Para
   r->gdiff.assign(np * 3, 0.f);
   r->filtered.assign(np * 3, 0.f);
   r->err.assign(np, 0.f);
+  r->gemis.assign(np * 3, 0.f);
+  r->direct.assign(np * 3, 0.f);
+  r->pot.assign(np, 0.f);
+  r->out.assign(np * 3, 0.f);
   r->sampleN.assign(np, 0u);
   r->counts.assign(np, 0u);
   r->cache.clear();
@@ -807,11 +865,13 @@ void bilateral(const float* color, const float* pos, const float* norm, const fl
 
 template <typename R>
 static void trace_pixels(Renderer* r, const Scene& s, const CamF& c, const std::vector<uint32_t>& pixOf,
-                         const std::vector<uint32_t>& sampleOf, std::vector<PathResult>& res, bool specPush) {
+                         const std::vector<uint32_t>& sampleOf, std::vector<PathResult>& res, bool specPush,
+                         bool bilat = false, bool pt = false) {
   const uint32_t n = (uint32_t)pixOf.size();
   res.assign(n, PathResult{});
   const uint32_t W = r->W;
-  const uint32_t chunk = 4096;
+  // ~8 chunks per thread: small samples still use every core
+  const uint32_t chunk = std::max<uint32_t>(64u, (n + r->threads * 8 - 1) / (r->threads * 8));
   uint32_t nchunks = (n + chunk - 1) / chunk;
   parallel_rows(nchunks, r->threads, [&](uint32_t ck) {
     uint32_t e = std::min(n, (ck + 1) * chunk);
@@ -823,9 +883,84 @@ static void trace_pixels(Renderer* r, const Scene& s, const CamF& c, const std::
       draw8(r->p.seed, r->p.request_id, pix, r->frame, kCamera, 0, smp, u);
       V<R> o, d;
       camera_ray<R>(c, x, y, u[0], u[1], &o, &d);
-      eye_path<R>(s, r->p, r->cache.data(), r->cacheSize, o, d, pix, r->frame, smp, specPush, &res[i]);
+      eye_path<R>(s, r->p, r->cache.data(), r->cacheSize, o, d, pix, r->frame, smp, specPush, bilat, pt, &res[i]);
     }
   });
+}
+
+// Filter-only mode ("BDPTSC Bilaterial", src/cudaRTBDPTStreamBilat.cu:1160-1461):
+// while frame < "Render Iteration" (0: always) one path per pixel with the
+// running means of pt_applyPathQueueResult_kernel (:989-1051: no inf test;
+// direct light and 1 - potential as running means; first-hit planes are the
+// frame's own), then the posnormemit filter with the diffuse plane as the
+// third feature, "Filter Iteration" passes, and the debug view.  The "Prob"
+// views filter max(minProb, mean potential) without overwriting the result
+// (the reference writes that view into its accumulator, :933-940).
+static void render_bilat(Renderer* r, const Scene& s, const CamF& c) {
+  const uint32_t np = r->W * r->H;
+  const uint32_t RI = r->p.render_iterations;
+  r->lastPaths = r->lastRays = r->lastNodes = r->lastTris = 0;
+  r->lastExt[0] = r->lastExt[1] = r->lastExt[2] = 0;
+  if (RI == 0 || r->frame < RI) {
+    if (r->frame % r->p.light_every == 0) light_pass(r, s, r->frame);
+    std::vector<uint32_t> pixOf(np), sampleOf(np, 0u);
+    for (uint32_t i = 0; i < np; i++) pixOf[i] = i;
+    std::vector<PathResult> res;
+    trace_pixels<float>(r, s, c, pixOf, sampleOf, res, false, true);
+    r->lastPaths = res.size();
+    for (auto& q : res) {
+      r->lastRays += q.rays;
+      r->lastNodes += q.nodes;
+      r->lastTris += q.tris;
+      r->lastExt[0] += q.extRays;
+      r->lastExt[1] += q.extNodes;
+      r->lastExt[2] += q.extTris;
+    }
+    const bool frame0 = r->frame == 0;
+    for (uint32_t i = 0; i < np; i++) {
+      const PathResult& q = res[i];
+      if (q.n == 0) continue;
+      if (frame0) r->sampleN[i] = 0;
+      const uint32_t old = r->sampleN[i], nn = old + q.n;
+      if (!(nn > old)) continue;
+      const float rInf = 1.f / (float)nn, oInf = (float)old * rInf;
+      for (int k = 0; k < 3; k++)
+        r->result[i * 3 + k] = std::fmax(rInf * (float)q.acc[k] + oInf * r->result[i * 3 + k], 0.f);
+      r->pot[i] = std::fmax(rInf * (1.f - (float)q.pot) + oInf * r->pot[i], 0.f);
+      r->sampleN[i] = nn;
+      for (int k = 0; k < 3; k++) {
+        r->direct[i * 3 + k] = rInf * (float)q.direct[k] + oInf * r->direct[i * 3 + k];
+        r->gpos[i * 3 + k] = (float)q.gpos[k];
+        r->gnorm[i * 3 + k] = (float)q.gnorm[k];
+        r->gemis[i * 3 + k] = (float)q.gemis[k];
+        r->gdiff[i * 3 + k] = (float)q.gdiff[k];
+      }
+    }
+  }
+  float gt[64];
+  const float delta = r->p.filter_sigma_spatial > 0.f ? r->p.filter_sigma_spatial : r->p.bilat_color_eud;
+  gaussian_table(delta, r->p.bilat_radius, gt);
+  std::vector<float> view;
+  const float* src = r->result.data();
+  const uint32_t dm = r->debug_mode;
+  if (dm == 2 || dm == 3) {
+    const float mp = dm == 3 ? r->p.min_trace_prob : 0.f;
+    view.resize((size_t)np * 3);
+    for (uint32_t i = 0; i < np; i++) view[i * 3] = view[i * 3 + 1] = view[i * 3 + 2] = std::fmax(mp, r->pot[i]);
+    src = view.data();
+  }
+  const Params& p = r->p;
+  bilateral(src, r->gpos.data(), r->gnorm.data(), r->gdiff.data(), r->W, r->H, p.bilat_color_eud, p.bilat_pos_eud,
+            p.bilat_norm_eud, p.bilat_diff_eud, p.bilat_radius, gt, r->filtered.data());
+  std::vector<float> tmp((size_t)np * 3);
+  for (uint32_t it = 1; it < p.filter_iterations; it++) {
+    bilateral(r->filtered.data(), r->gpos.data(), r->gnorm.data(), r->gdiff.data(), r->W, r->H, p.bilat_color_eud,
+              p.bilat_pos_eud, p.bilat_norm_eud, p.bilat_diff_eud, p.bilat_radius, gt, tmp.data());
+    r->filtered.swap(tmp);
+  }
+  const std::vector<float>& o = dm == 4 ? r->direct : dm == 5 ? r->gpos : dm == 6 ? r->gnorm
+                                : dm == 7 ? r->result : r->filtered;
+  r->out = o;
 }
 
 void render_frame(Renderer* r, const Scene& s, const Camera& cam) {
@@ -847,6 +982,38 @@ void render_frame(Renderer* r, const Scene& s, const Camera& cam) {
   std::copy(basis9, basis9 + 9, r->camBasis);
   r->started = true;
   const uint32_t np = r->W * r->H;
+  if (r->mode == kModeBilat) {
+    render_bilat(r, s, c);
+    return;
+  }
+  if (r->mode == kModePT) {  // cudaRTPTStream::Render (src/cudaRTPTStream.cu:380-431): no light pass
+    std::vector<uint32_t> pixOf(np), sampleOf(np, 0u);
+    for (uint32_t i = 0; i < np; i++) pixOf[i] = i;
+    std::vector<PathResult> res;
+    trace_pixels<float>(r, s, c, pixOf, sampleOf, res, false, false, true);
+    r->lastPaths = res.size();
+    r->lastRays = r->lastNodes = r->lastTris = 0;
+    r->lastExt[0] = r->lastExt[1] = r->lastExt[2] = 0;
+    for (auto& q : res) {
+      r->lastRays += q.rays;
+      r->lastNodes += q.nodes;
+      r->lastTris += q.tris;
+      r->lastExt[0] += q.extRays;
+      r->lastExt[1] += q.extNodes;
+      r->lastExt[2] += q.extTris;
+    }
+    // pt_applyPathQueueResult_kernel (:335-358): frame-count weights, no inf test
+    const float rInf = 1.f / (float)(r->frame + 1), oInf = 1.f - rInf;
+    for (uint32_t i = 0; i < np; i++) {
+      if (res[i].n == 0) continue;
+      for (int k = 0; k < 3; k++) {
+        const float smp = (float)res[i].acc[k] / (float)res[i].n;
+        r->result[i * 3 + k] = std::fmax(rInf * smp + oInf * r->result[i * 3 + k], 0.f);
+      }
+      r->sampleN[i] = r->frame + 1;
+    }
+    return;
+  }
   if (r->frame % r->p.light_every == 0) light_pass(r, s, r->frame);
 
   const bool adaptive = r->mode == kModeAdaptive || r->mode == kModeAdaptiveBinary;
@@ -939,10 +1106,14 @@ void render_frame(Renderer* r, const Scene& s, const Camera& cam) {
   trace_pixels<float>(r, s, c, pixOf, sampleOf, res, r->mode == kModeAdaptive);  // spec push: PLL variant only
   r->lastPaths = res.size();
   r->lastRays = r->lastNodes = r->lastTris = 0;
+  r->lastExt[0] = r->lastExt[1] = r->lastExt[2] = 0;
   for (auto& q : res) {
     r->lastRays += q.rays;
     r->lastNodes += q.nodes;
     r->lastTris += q.tris;
+    r->lastExt[0] += q.extRays;
+    r->lastExt[1] += q.extNodes;
+    r->lastExt[2] += q.extTris;
   }
   float* g3[3] = {r->gpos.data(), r->gnorm.data(), r->gdiff.data()};
   if (!uniform && binary) {  // pt_applyPathQueueResult_kernel per pass, in pass order (:1396-1418)

@@ -29,9 +29,19 @@ struct Params {
   float filter_sigma_spatial;  // <= 0: the reference's quirk (spatial table from the colour delta)
   uint32_t request_id;       // Philox key word 1
   float min_trace_prob;      // "Min Trace Probability" (AdapBilatBinary.cu:28), binary allocator
+  // filter-only mode, src/cudaRTBDPTStreamBilat.cu:29-37
+  float bilat_color_eud;     // "Filter Color E Delta" 1
+  float bilat_pos_eud;       // "Filter Pos E Delta" 1
+  float bilat_norm_eud;      // "Filter Norm E Delta" 1
+  float bilat_emit_eud;      // "Filter Emit E Delta" 0.5 (not read by the filter call)
+  float bilat_diff_eud;      // "Filter Diff E Delta" 0.5
+  uint32_t bilat_radius;     // "Filter Radius" 5
+  uint32_t filter_iterations;  // "Filter Iteration" 1
+  uint32_t render_iterations;  // "Render Iteration" 5 (0: no limit)
+  uint32_t pt_depth_max;       // PTSC NORMALRAY_BOUND_MAX (src/cudaRTPTStream.cu:6) 10
 };
 
-enum Mode : int32_t { kModeBDPT = 0, kModeAdaptive = 1, kModeAdaptiveBinary = 2 };
+enum Mode : int32_t { kModeBDPT = 0, kModeAdaptive = 1, kModeAdaptiveBinary = 2, kModeBilat = 3, kModePT = 4 };
 
 struct Camera {
   float pos[3], dir[3], up[3];
@@ -47,8 +57,13 @@ struct PathResult {  // per finished camera path
   double acc[3];
   uint32_t n;
   double gpos[3], gnorm[3], gdiff[3];  // first-hit G-buffer (adaptive variant)
+  double gemis[3];                     // first-hit emissive (filter-only mode)
+  double direct[3];                    // direct-light sample (filter-only mode)
+  double pot;                          // path potential at termination (filter-only mode)
   uint32_t rays;                       // extension + shadow rays traced
   uint64_t nodes, tris;                // traversal work (algorithmic byte count)
+  uint32_t extRays;                    // of which extension (closest-hit) walks
+  uint64_t extNodes, extTris;
 };
 
 struct Renderer {
@@ -60,6 +75,8 @@ struct Renderer {
   bool started = false;
   float camBasis[9] = {0};  // pos, dir, up after orthonormalisation
   std::vector<float> result, gpos, gnorm, gdiff, filtered, err;
+  std::vector<float> gemis, direct, pot, out;  // filter-only mode; `out` = the view gbpt_render copies
+  uint32_t debug_mode = 0;                     // filter-only mode "Debug Mode" (0..7)
   std::vector<uint32_t> sampleN, counts;
   std::vector<uint32_t> chunks;  // binary allocator: paths per pass (last = fill)
   std::vector<LightVertex> cache;
@@ -69,6 +86,7 @@ struct Renderer {
   uint32_t x0 = 0, y0 = 0, fullW = 0, fullH = 0;
   // statistics of the last frame
   uint64_t lastPaths = 0, lastRays = 0, lastNodes = 0, lastTris = 0;
+  uint64_t lastExt[3] = {0, 0, 0};  // extension rays, node visits, triangle tests
 };
 
 void default_params(Params* p);

@@ -92,7 +92,8 @@ void orc_render(void* rp, void* sp, const float* cam, uint32_t frames) {
   for (uint32_t f = 0; f < frames; f++) render_frame(r, *(Scene*)sp, c);
 }
 
-// which: 0 result, 1 position, 2 normal, 3 diffuse, 4 filtered, 5 error (W*H)
+// which: 0 result, 1 position, 2 normal, 3 diffuse, 4 filtered, 5 error (W*H),
+// filter-only mode: 8 direct, 9 first-hit emissive, 10 mean 1 - potential (W*H), 11 the debug view
 void orc_renderer_get(void* rp, int32_t which, float* out) {
   Renderer* r = (Renderer*)rp;
   const std::vector<float>* src = nullptr;
@@ -103,10 +104,15 @@ void orc_renderer_get(void* rp, int32_t which, float* out) {
     case 3: src = &r->gdiff; break;
     case 4: src = &r->filtered; break;
     case 5: src = &r->err; break;
+    case 8: src = &r->direct; break;
+    case 9: src = &r->gemis; break;
+    case 10: src = &r->pot; break;
+    case 11: src = &r->out; break;
     default: return;
   }
   std::memcpy(out, src->data(), src->size() * 4);
 }
+void orc_renderer_set_debug(void* rp, uint32_t mode) { ((Renderer*)rp)->debug_mode = mode; }
 void orc_renderer_counts(void* rp, uint32_t* sampleN, uint32_t* counts) {
   Renderer* r = (Renderer*)rp;
   if (sampleN) std::memcpy(sampleN, r->sampleN.data(), r->sampleN.size() * 4);
@@ -119,6 +125,10 @@ void orc_renderer_stats(void* rp, uint64_t* out4) {
   out4[1] = r->lastRays;
   out4[2] = r->lastNodes;
   out4[3] = r->lastTris;
+}
+void orc_renderer_ext_stats(void* rp, uint64_t* out3) {
+  Renderer* r = (Renderer*)rp;
+  for (int k = 0; k < 3; k++) out3[k] = r->lastExt[k];
 }
 uint32_t orc_renderer_light_cache(void* rp, float* out) {  // 21 floats per vertex
   Renderer* r = (Renderer*)rp;

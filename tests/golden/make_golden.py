@@ -10,6 +10,10 @@ Outputs (all produced by the CPU oracle, FP32 float contract):
   obj_cornell.npz   mesh, BVH (bounds/offsets/order) and 1024 traced rays
   cornell_frames.npz 3 progressive frames of a 24x24 plain-BDPT render and
                      the light-vertex cache of frame 0
+  obj_cornell_glass.npz the OBJ with its MTL materials, the sphere made glass
+                     as the reference's cornellwtranball preset does, and that
+                     preset's camera (a scene with refraction and total
+                     internal reflection)
 The Philox4x32-10 known-answer vectors are the published Random123 ones and
 live in the test itself.
 """
@@ -56,6 +60,17 @@ def main(ref_root):
     np.savez_compressed(os.path.join(HERE, "cornell_frames.npz"), vertices=v2, triangles=t2, materials=m2,
                         cam=oracle.cam_array(cam), params=params, frames=np.array(frames), cache=cache,
                         sampleN=r.sample_counts()[0])
+    # the same OBJ with its MTL materials and the preset's glass sphere
+    # (asset/preset/cornellwtranball.NPRTENV: transparency 1, roughness 0) and camera
+    from cudapt_gb300 import preset
+    v3, t3, m3 = objio.load_obj(obj, with_materials=True)
+    pre = preset.load(os.path.join(HERE, "cornellwtranball.NPRTENV"))
+    glass = int(np.argmax(np.bincount(t3["mat"])))  # the sphere holds most triangles
+    m3[glass]["transparency"] = 1.0
+    m3[glass]["roughness"] = 0.0
+    cam3 = pre["camera"]
+    np.savez_compressed(os.path.join(HERE, "obj_cornell_glass.npz"), vertices=v3, triangles=t3, materials=m3,
+                        cam=oracle.cam_array(cam3))
     print("wrote", os.listdir(HERE))
 
 

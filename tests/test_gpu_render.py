@@ -98,6 +98,31 @@ def test_interior_plain_matches(gbdev, orc):
     assert np.abs(img.mean() - want.mean()) <= 1e-3 * max(want.mean(), 1e-6)
 
 
+def test_walk_counters_match_oracle(gbdev, orc):
+    """Closest-hit rays, node visits and triangle tests of a whole frame
+    (wavefront and tail kernels) equal the oracle's counts for the same
+    paths: the persistent walks visit nodes in TracePrimitive's order.  The
+    kernels skip connection rays whose contribution is zero whatever their
+    visibility, so their any-hit work is at most the oracle's."""
+    (v, t, m), cam = scene_arrays("interior")
+    W, H = 80, 60
+    params = gbdev.default_params(eye_depth_max=10, light_depth_max=10)
+    s = gbdev.RTScene(v, t, m).build_bvh()
+    r = gbdev.RTRenderer(W, H, 0, params)
+    r.set_counting(True)
+    r.render(s, cam)
+    st = r.render_frames(s, cam, 1)
+    ref = orc.Renderer(W, H, 0, params)
+    ref.render(orc.Scene(v, t, m), cam, 2)
+    rs = ref.stats()
+    assert st["paths"] == rs["paths"] == W * H
+    for got, want in ((st["rays"] - st["shadow_rays"], rs["ext_rays"]), (st["nodes"], rs["ext_nodes"]),
+                      (st["tris"], rs["ext_tris"])):
+        assert abs(int(got) - int(want)) <= 2e-3 * want, (got, want)
+    assert st["shadow_rays"] <= (rs["rays"] - rs["ext_rays"]) * 1.002
+    assert st["shadow_nodes"] <= (rs["nodes"] - rs["ext_nodes"]) * 1.002
+
+
 def test_env_term(gbdev, orc):
     """Constant environment on a miss (scene open at z=1: Cornell)."""
     r, ref, img, want, _ = _render_both(gbdev, orc, "cornell", 48, 48, 3, eye_depth_max=8, light_depth_max=8,

@@ -14,7 +14,7 @@ def test_reference_preset_parses():
     d = preset.load(os.path.join(GOLD, "cornellwtranball.NPRTENV"))
     assert d["campos"] == (-1.82495, -2.40754, -2.74389)
     assert (d["pitch"], d["yaw"]) == (-0.13, -0.215)
-    assert d["rttech"] == 3 and preset.RTTECH_NAMES[3] == "PTSC" and d["mode"] is None
+    assert d["rttech"] == 3 and preset.RTTECH_NAMES[3] == "PTSC" and d["mode"] == layouts.MODE_PT_SC
     assert d["models"] == ["..\\asset\\model\\cornell_box_with_sphere.obj"]
     m = d["materials"]
     assert len(m) == 6

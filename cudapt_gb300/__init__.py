@@ -153,6 +153,20 @@ class RTRenderer:
     def handle(self):
         return self._h
 
+    def set_mlp(self, mlp=None, collect=False):
+        """Learned allocation with `mlp` (cudapt_gb300.mlp.MLP) in the PLL adaptive mode;
+        collect=True keeps the feature statistics without changing the allocation."""
+        self._mlp = mlp  # keep the network alive while attached
+        check(load().gbpt_renderer_set_mlp(self._h, mlp.handle if mlp is not None else None, int(bool(collect))))
+
+    def features(self):
+        """(tiles, 24) features of the current statistics (row-major 8x8 tiles)."""
+        n = ctypes.c_uint32()
+        check(load().gbpt_renderer_features(self._h, None, 0, 0, ctypes.addressof(n)))
+        out = np.zeros((n.value, 24), np.float32)
+        check(load().gbpt_renderer_features(self._h, ptr(out), n.value, 0, ctypes.addressof(n)))
+        return out
+
     def rmse(self, converged):
         """RMSE of the current image against a converged W*H*3 image (on the GPU)."""
         from .experiment import renderer_rmse
@@ -207,6 +221,8 @@ class RTRenderer:
         np_ = self.width * self.height
         if which in (5, 10):
             out = np.zeros(np_, np.float32)
+        elif which == 12:
+            out = np.zeros(((self.width + 7) // 8) * ((self.height + 7) // 8) * 8, np.uint32)
         elif which == 6:
             out = np.zeros(np_, np.uint32)
         else:

@@ -92,6 +92,16 @@ SIGNATURES = {
     "gbpt_rmse": (i32, [vp, vp, ctypes.c_uint64, i32, vp]),
     "gbpt_renderer_rmse": (i32, [vp, vp, i32, vp]),
     "gbpt_tonemap_rgba8": (i32, [vp, vp, u32, u32, f32, i32, vp, i32]),
+    "gbpt_mlp_param_count": (u32, []),
+    "gbpt_mlp_create": (i32, [u32, vp]),
+    "gbpt_mlp_destroy": (i32, [vp]),
+    "gbpt_mlp_get_params": (i32, [vp, vp]),
+    "gbpt_mlp_set_params": (i32, [vp, vp]),
+    "gbpt_mlp_forward": (i32, [vp, vp, u32, vp, i32]),
+    "gbpt_mlp_gradients": (i32, [vp, vp, vp, u32, i32, vp, vp]),
+    "gbpt_mlp_train_step": (i32, [vp, vp, vp, u32, f32, i32, vp]),
+    "gbpt_renderer_set_mlp": (i32, [vp, vp, i32]),
+    "gbpt_renderer_features": (i32, [vp, vp, u32, i32, vp]),
     "gbpt_fmath": (i32, [i32, vp, u32, vp]),
     "gbpt_philox": (i32, [vp, u32, u32, u32, vp]),
 }

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgbpt.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels_wave.cu", "kernels_adapt.cu", "api.cu", "noalloc.cu", "image.cu", "bvh_build.cpp"]
+SOURCES = ["kernels_wave.cu", "kernels_adapt.cu", "api.cu", "noalloc.cu", "image.cu", "mlp.cu", "bvh_build.cpp"]
 
 
 def _nvcc():

@@ -185,6 +185,9 @@ struct gbpt_renderer {
   // filter-only mode: first-hit emissive, direct-light and 1 - potential means,
   // the second ping-pong filter plane and the "Prob" view scratch plane
   float *gemis = nullptr, *direct = nullptr, *pot = nullptr, *filtered2 = nullptr, *probView = nullptr;
+  // learned allocator: the attached network (not owned), whether statistics are kept without one
+  gbpt_mlp* mlp = nullptr;
+  bool collect = false;
   const float* bilatOut = nullptr;  // filter plane holding the last filtered image
   uint32_t* sampleN = nullptr;
   float4* waveMem = nullptr;
@@ -241,6 +244,11 @@ struct gbpt_renderer {
     dfree(pot);
     dfree(filtered2);
     dfree(probView);
+    dfree(rb.m2);
+    dfree(rb.hist);
+    dfree(ab.feat);
+    dfree(ab.pred);
+    dfree(ab.tileErr);
     bilatOut = nullptr;
     dfree(gauss);
     dfree(sampleN);
@@ -314,6 +322,14 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   CK(dalloc(&r->pot, np));
   CK(dalloc(&r->filtered2, np * 3));
   CK(dalloc(&r->probView, np * 3));
+  const size_t nTiles = (size_t)((r->W + 7) / 8) * ((r->H + 7) / 8);
+  CK(dalloc(&r->rb.m2, np * 3));
+  CK(dalloc(&r->rb.hist, nTiles * 8));
+  CK(dalloc(&r->ab.feat, nTiles * kFeatures));
+  CK(dalloc(&r->ab.pred, nTiles));
+  CK(dalloc(&r->ab.tileErr, nTiles));
+  CK(cudaMemsetAsync(r->rb.m2, 0, np * 12, r->st));
+  CK(cudaMemsetAsync(r->rb.hist, 0, nTiles * 32, r->st));
   CK(dalloc(&r->sampleN, np));
   CK(dalloc(&r->gauss, 64));
   CK(dalloc(&r->ab.err, np));
@@ -454,6 +470,12 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   const bool bilat = r->mode == GBPT_MODE_BDPT_SC_BILAT;
   a.gbuffer = (adaptive || bilat) ? 1u : 0u;
   a.bilat = bilat ? 1u : 0u;
+  // learned allocator (PLL adaptive mode): second moments and path-length counts
+  const bool learned = r->mlp != nullptr && r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT;
+  a.moments = (learned || (r->collect && adaptive)) ? 1u : 0u;
+  a.tilesX = (r->W + 7) / 8;
+  if (a.moments && r->frame == 0)
+    CK(cudaMemsetAsync(r->rb.hist, 0, (size_t)a.tilesX * ((r->H + 7) / 8) * 32, r->st));
   a.counting = r->counting ? 1u : 0u;
   const DevScene& S = s->dev;
   cudaStream_t st = r->st;
@@ -510,7 +532,16 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
     mark(r, kPhFilter, timing);
     if (binary)
       CK(launch_binary_budget(a, r->rb, r->ab, r->result, r->sampleN, r->p.desired_n, r->p.min_trace_prob, st));
-    else
+    else if (learned) {  // heuristic error -> tile features -> MLP -> per-pixel weights -> budget
+      CK(launch_adapt_error(a, r->ab, r->result, r->sampleN, r->p.desired_n, st));
+      CK(launch_tile_features(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
+      const uint32_t nTiles = a.tilesX * ((r->H + 7) / 8);
+      gbpt_status ms = mlp_forward_async(r->mlp, r->ab.feat, nTiles, r->ab.pred, &r->rb.ctr->errFlags,
+                                         kErrMlpTimeout, st);
+      if (ms != GBPT_OK) return ms;
+      CK(launch_mlp_alloc(a, r->ab, st));
+      CK(launch_adapt_alloc(a, r->rb, r->ab, st));
+    } else
       CK(launch_adapt_budget(a, r->rb, r->ab, r->result, r->sampleN, r->p.desired_n, st));
     mark(r, kPhAdapt, timing);
   } else {
@@ -609,6 +640,7 @@ gbpt_status render_impl(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam,
     if (flags) {
       CK(cudaMemset(&r->rb.ctr->errFlags, 0, 4));
       if (flags & 4u) return fail(GBPT_ERR_TIMEOUT, "grid barrier of the binary allocator timed out");
+      if (flags & kErrMlpTimeout) return fail(GBPT_ERR_TIMEOUT, "learned allocator: tensor-core wait timed out");
       return fail(GBPT_ERR_BOUNDS, "device bounds check tripped (light cache)");
     }
   }
@@ -1003,6 +1035,8 @@ gbpt_status gbpt_read_buffer(gbpt_renderer* r, int32_t which, void* dst, size_t 
     case 8: src = r->direct; break;
     case 9: src = r->gemis; break;
     case 10: src = r->pot; need = np * 4; break;
+    case 11: src = r->rb.m2; break;
+    case 12: src = r->rb.hist; need = (size_t)((r->W + 7) / 8) * ((r->H + 7) / 8) * 32; break;
     case 7: {  // light-vertex cache in the 21-float layout of the reference's LightVertex
       DevCounters c{};
       gbpt_status st = read_ctr(r, &c);
@@ -1050,6 +1084,44 @@ gbpt_status gbpt_renderer_rmse(gbpt_renderer* r, const float* converged, int32_t
   cudaStreamSynchronize(r->st);
   dfree(d);
   return st;
+}
+
+gbpt_status gbpt_renderer_set_mlp(gbpt_renderer* r, gbpt_mlp* mlp, int32_t collect) {
+  if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
+  r->mlp = mlp;
+  r->collect = collect != 0;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_renderer_features(gbpt_renderer* r, float* out, uint32_t capacity, int32_t out_is_device,
+                                   uint32_t* n_tiles) {
+  if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
+  const uint32_t tilesX = (r->W + 7) / 8, nTiles = tilesX * ((r->H + 7) / 8);
+  if (n_tiles) *n_tiles = nTiles;
+  if (!out) return GBPT_OK;
+  if (capacity < nTiles) return fail(GBPT_ERR_INVALID_ARG, "feature buffer too small");
+  if (!r->alloc || !r->started) return fail(GBPT_ERR_STATE, "renderer has not rendered yet");
+  if (r->mode != GBPT_MODE_BDPT_SC_ADAP_BILAT && r->mode != GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY)
+    return fail(GBPT_ERR_STATE, "features need an adaptive mode (first-hit planes)");
+  cudaStream_t st = r->st;
+  FrameArgs a{};
+  a.width = r->W;
+  a.height = r->H;
+  a.tilesX = tilesX;
+  a.moments = 1;
+  for (int k = 0; k < 3; k++) a.camPos[k] = r->camBasis[k];
+  const float delta = r->p.filter_sigma_spatial > 0.f ? r->p.filter_sigma_spatial : r->p.filter_color_eud;
+  gbpt_status ge = ensure_gauss(r, delta, r->p.filter_radius, st);
+  if (ge != GBPT_OK) return ge;
+  CK(launch_bilateral(r->result, r->gpos, r->gnorm, r->p.filter_diffuse ? r->gdiff : nullptr, r->W, r->H,
+                      r->p.filter_color_eud, r->p.filter_pos_eud, r->p.filter_norm_eud, r->p.filter_diff_eud,
+                      r->p.filter_radius, r->gauss, r->ab.filtered, st));
+  CK(launch_adapt_error(a, r->ab, r->result, r->sampleN, r->p.desired_n, st));
+  CK(launch_tile_features(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
+  CK(cudaMemcpyAsync(out, r->ab.feat, (size_t)nTiles * kFeatures * 4,
+                     out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return GBPT_OK;
 }
 
 gbpt_status gbpt_reset(gbpt_renderer* r) {

@@ -24,6 +24,11 @@ bool build_bvh(const gbpt_vertex* verts, const gbpt_triangle* tris, uint32_t nt,
 // `stream` (a cudaStream_t); image.cu
 gbpt_status rmse_device(const float* a, const float* b, uint64_t n, double* out, void* stream);
 
+// MLP inference on device arrays on `stream` (mlp.cu); a tensor-core wait that
+// runs out ORs errBit into *err
+gbpt_status mlp_forward_async(gbpt_mlp* m, const float* x, uint32_t n, float* y, uint32_t* err, uint32_t errBit,
+                              void* stream);
+
 // thread-local error text (gbpt_last_error_string)
 void set_error(const std::string& s);
 gbpt_status fail(gbpt_status st, const std::string& s);

@@ -312,7 +312,7 @@ __global__ void k_accum(FrameArgs a, RenderBuffers b, const uint32_t* __restrict
   const uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t lane = threadIdx.x & 31;
   if (p >= np) return;  // warp-uniform
-  float v[12] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float v[15] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   uint32_t tN = 0;
   const uint32_t o = off[p], c = cnt[p];
   for (uint32_t s = o + lane; s < o + c; s += 32) {
@@ -325,9 +325,12 @@ __global__ void k_accum(FrameArgs a, RenderBuffers b, const uint32_t* __restrict
     v[3] = v[3] + g0.x * fn; v[4] = v[4] + g0.y * fn; v[5] = v[5] + g0.z * fn;
     v[6] = v[6] + g1.x * fn; v[7] = v[7] + g1.y * fn; v[8] = v[8] + g1.z * fn;
     v[9] = v[9] + g2.x * fn; v[10] = v[10] + g2.y * fn; v[11] = v[11] + g2.z * fn;
+    if (a.moments) {  // second moments for the learned allocator's features
+      v[12] = v[12] + (r.x * r.x) / fn; v[13] = v[13] + (r.y * r.y) / fn; v[14] = v[14] + (r.z * r.z) / fn;
+    }
     tN += n;
   }
-  for (int k = 0; k < 12; k++) v[k] = bfly(v[k]);
+  for (int k = 0; k < (a.moments ? 15 : 12); k++) v[k] = bfly(v[k]);
   for (int m = 16; m > 0; m >>= 1) tN += __shfl_xor_sync(0xffffffffu, tN, m);
   if (lane != 0) return;
   float* q = result + 3 * (size_t)p;
@@ -342,6 +345,10 @@ __global__ void k_accum(FrameArgs a, RenderBuffers b, const uint32_t* __restrict
   const uint32_t nn = tN + N;
   if (nn > N) {
     const float rInf = 1.f / (float)nn, oInf = (float)N * rInf;
+    if (a.moments) {
+      float* m = b.m2 + 3 * (size_t)p;
+      for (int k = 0; k < 3; k++) m[k] = N ? rInf * v[12 + k] + oInf * m[k] : rInf * v[12 + k];
+    }
     for (int k = 0; k < 3; k++) {
       q[k] = fmaxf(rInf * v[k] + oInf * q[k], 0.f);
       P[k] = rInf * v[3 + k] + oInf * P[k];
@@ -628,17 +635,139 @@ cudaError_t launch_bilateral(const float* color, const float* pos, const float* 
   return cudaGetLastError();
 }
 
-cudaError_t launch_adapt_budget(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab,
-                                const float* result, const uint32_t* sampleN, uint32_t desired, cudaStream_t st) {
+cudaError_t launch_adapt_error(const FrameArgs& a, const AdaptBuffers& ab, const float* result,
+                               const uint32_t* sampleN, uint32_t desired, cudaStream_t st) {
+  const uint32_t np = a.width * a.height;
+  k_error<<<adapt_reduce_blocks(np), kReduceBlock, 0, st>>>(ab.filtered, result, sampleN, np, desired, ab.err,
+                                                             ab.partial);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adapt_alloc(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab, cudaStream_t st) {
   const uint32_t np = a.width * a.height;
   const uint32_t nr = adapt_reduce_blocks(np), ns = adapt_scan_blocks(np);
-  k_error<<<nr, kReduceBlock, 0, st>>>(ab.filtered, result, sampleN, np, desired, ab.err, ab.partial);
   k_reduce_final<<<1, 1024, 0, st>>>(ab.partial, nr, b.ctr);
   k_budget<<<ns, kScanBlock, 0, st>>>(ab.err, np, b.ctr, ab.cnt, ab.off, ab.blockSum);
   k_scan_blocks<<<1, 1024, 0, st>>>(ab.blockSum, ns, np, b.ctr);
   k_offsets<<<(np + 255) / 256, 256, 0, st>>>(ab.off, ab.cnt, ab.blockSum, np, np);
   k_gen_adapt<<<sm_count() * 8, 256, 0, st>>>(a, b, ab.off, ab.cnt);
-  note_launches(6);
+  note_launches(5);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adapt_budget(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab,
+                                const float* result, const uint32_t* sampleN, uint32_t desired, cudaStream_t st) {
+  cudaError_t e = launch_adapt_error(a, ab, result, sampleN, desired, st);
+  return e == cudaSuccess ? launch_adapt_alloc(a, b, ab, st) : e;
+}
+
+// ---------------------------------------------------------------------------
+// Learned allocator.  Features of one 8x8 tile (edge tiles: the pixels that
+// exist), one warp per tile, lane l covering pixels l and l + 32:
+//   0-2   log(1 + mean colour)             3-5   log(1 + 100 * mean variance of the pixel means)
+//   6-8   mean first-hit albedo            9-11  mean first-hit normal
+//   12    log(1 + mean first-hit distance) 13-20 fraction of paths that ended after 0..7+ hits
+//   21    log2(1 + mean samples per pixel) 22/23 log(1 + 1000 * mean / max heuristic error)
+// The variance of a pixel mean is max(m2 - mean^2, 0) / n with m2 the running
+// mean of (path sum)^2 / (path count).
+__global__ void k_tile_features(FrameArgs a, RenderBuffers b, AdaptBuffers ab, const float* __restrict__ result,
+                                const uint32_t* __restrict__ sampleN, const float* __restrict__ gpos,
+                                const float* __restrict__ gnorm, const float* __restrict__ gdiff,
+                                uint32_t nTiles) {
+  const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  if (tile >= nTiles) return;  // warp-uniform
+  const uint32_t tx = tile % a.tilesX, ty = tile / a.tilesX;
+  float s[16];
+  for (int k = 0; k < 16; k++) s[k] = 0.f;
+  float emax = 0.f;
+  for (uint32_t h = 0; h < 2; h++) {
+    const uint32_t k = lane + 32u * h;
+    const uint32_t x = tx * 8u + (k & 7u), y = ty * 8u + (k >> 3);
+    if (x >= a.width || y >= a.height) continue;
+    const size_t p = (size_t)y * a.width + x;
+    const float n = (float)sampleN[p];
+    for (int c = 0; c < 3; c++) {
+      const float mu = result[3 * p + c];
+      const float var = n > 0.f ? fmaxf(b.m2[3 * p + c] - mu * mu, 0.f) / n : 0.f;
+      s[c] += mu;
+      s[3 + c] += var;
+      s[6 + c] += gdiff[3 * p + c];
+      s[9 + c] += gnorm[3 * p + c];
+    }
+    const float dx = gpos[3 * p] - a.camPos[0], dy = gpos[3 * p + 1] - a.camPos[1], dz = gpos[3 * p + 2] - a.camPos[2];
+    s[12] += sqrtf(dx * dx + dy * dy + dz * dz);
+    s[13] += n;
+    const float e = ab.err[p];
+    s[14] += e;
+    emax = fmaxf(emax, e);
+    s[15] += 1.f;
+  }
+  for (int k = 0; k < 16; k++)
+    for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
+  for (int o = 16; o > 0; o >>= 1) emax = fmaxf(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+  if (lane >= 8) return;
+  const uint32_t* hp = b.hist + tile * 8u;
+  uint32_t hsum = 0;
+  for (int k = 0; k < 8; k++) hsum += hp[k];
+  float* f = ab.feat + (size_t)tile * kFeatures;
+  const float inv = 1.f / fmaxf(s[15], 1.f);
+  if (lane == 0) {
+    for (int c = 0; c < 3; c++) {
+      f[c] = log1pf(fmaxf(s[c] * inv, 0.f));
+      f[3 + c] = log1pf(100.f * s[3 + c] * inv);
+      f[6 + c] = s[6 + c] * inv;
+      f[9 + c] = s[9 + c] * inv;
+    }
+    f[12] = log1pf(s[12] * inv);
+    f[21] = log2f(1.f + s[13] * inv);
+    f[22] = log1pf(1000.f * s[14] * inv);
+    f[23] = log1pf(1000.f * emax);
+    ab.tileErr[tile] = s[14];
+  }
+  f[13 + lane] = hsum ? (float)hp[lane] / (float)hsum : 0.f;
+}
+
+// e'_p = exp(pred[tile]) * e_p / (sum of e over the tile), or exp(pred) / pixels
+// when the tile's heuristic error is zero; FP64 partial sums as k_error's
+__global__ void __launch_bounds__(kReduceBlock) k_mlp_alloc(FrameArgs a, AdaptBuffers ab, uint32_t np) {
+  __shared__ double ws[kReduceBlock / 32];
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (p < np) {
+    const uint32_t x = p % a.width, y = p / a.width;
+    const uint32_t tile = (y >> 3) * a.tilesX + (x >> 3);
+    const float w = expf(fminf(fmaxf(ab.pred[tile], -30.f), 30.f));
+    const float S = ab.tileErr[tile];
+    const uint32_t tw = min(8u, a.width - (x & ~7u)), th = min(8u, a.height - (y & ~7u));
+    const float e = S > 0.f ? w * (ab.err[p] / S) : w / (float)(tw * th);
+    ab.err[p] = e;
+    v = (double)e;
+  }
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s2 = 0.0;
+    for (int w = 0; w < kReduceBlock / 32; w++) s2 += ws[w];
+    ab.partial[blockIdx.x] = s2;
+  }
+}
+
+cudaError_t launch_tile_features(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab,
+                                 const float* result, const uint32_t* sampleN, const float* gpos, const float* gnorm,
+                                 const float* gdiff, cudaStream_t st) {
+  const uint32_t nTiles = a.tilesX * ((a.height + 7) / 8);
+  k_tile_features<<<(nTiles * 32 + 255) / 256, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff, nTiles);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_alloc(const FrameArgs& a, const AdaptBuffers& ab, cudaStream_t st) {
+  const uint32_t np = a.width * a.height;
+  k_mlp_alloc<<<adapt_reduce_blocks(np), kReduceBlock, 0, st>>>(a, ab, np);
+  note_launches(1);
   return cudaGetLastError();
 }
 

@@ -451,6 +451,15 @@ struct PathIO {
   float4 shA, shB, shC;
 };
 
+// learned allocator statistics: a finished path of pixel `pix` after `hits`
+// surface hits, counted in its 8x8 tile's path-length histogram
+__device__ __forceinline__ void count_path_length(const FrameArgs& a, const RenderBuffers& b, uint32_t pix,
+                                                  uint32_t hits) {
+  const uint32_t px = pix % a.width, py = pix / a.width;
+  const uint32_t tile = (py >> 3) * a.tilesX + (px >> 3);
+  atomicAdd(&b.hist[tile * 8u + (hits < 7u ? hits : 7u)], 1u);
+}
+
 __device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a, const RenderBuffers& b,
                                            const float4* __restrict__ cache, uint32_t cacheSize, uint32_t depth,
                                            float4 h4, PathIO& io) {
@@ -467,6 +476,7 @@ __device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a
     b.res[slot] = make_float4(r.x + pathSample.x, r.y + pathSample.y, r.z + pathSample.z,
                               __uint_as_float(__float_as_uint(r.w) + 1u));
     if (a.bilat) reinterpret_cast<float*>(b.dsm + slot)[3] = pot;
+    if (a.moments) count_path_length(a, b, pix, depth);
     return;
   }
   const uint32_t smp = b.slotSmp[slot];
@@ -499,6 +509,7 @@ __device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a
     b.res[slot] = make_float4(r.x + pathSample.x, r.y + pathSample.y, r.z + pathSample.z,
                               __uint_as_float(__float_as_uint(r.w) + 1u));
     if (a.bilat) reinterpret_cast<float*>(b.dsm + slot)[3] = pot;
+    if (a.moments) count_path_length(a, b, pix, depth + 1);
     return;
   }
   io.cont = true;
@@ -724,6 +735,14 @@ __global__ void k_apply(FrameArgs a, RenderBuffers b, float* result, uint32_t* s
   q[1] = fmaxf(rInf * r.y + oInf * q[1], 0.f);
   q[2] = fmaxf(rInf * r.z + oInf * q[2], 0.f);
   sampleN[p] = nn;
+  if (a.moments) {  // running mean of acc^2 / n (the path's second moment weighted like its mean)
+    const float fn = (float)n;
+    float* m = b.m2 + 3 * (size_t)p;
+    const float s0 = (r.x * r.x) / fn, s1 = (r.y * r.y) / fn, s2 = (r.z * r.z) / fn;
+    m[0] = old ? rInf * s0 + oInf * m[0] : rInf * s0;
+    m[1] = old ? rInf * s1 + oInf * m[1] : rInf * s1;
+    m[2] = old ? rInf * s2 + oInf * m[2] : rInf * s2;
+  }
   if (gpos) {
     float* planes[3] = {gpos, gnorm, gdiff};
     const float fn = (float)n;
@@ -829,12 +848,12 @@ __global__ void k_trace_rays(DevScene S, const float* rays, uint32_t n, float ma
 int g_sm = 0;
 
 // Idle lanes of a warp that trigger a refill in k_walk / k_tail (tuning
-// knob, GBPT_WALK_REFILL, 1..32; 24 by default: refilling only when most
-// lanes are idle keeps lanes that started together on nearby rays).
+// knob, GBPT_WALK_REFILL, 1..32; 20 by default: measured 16-20 best on the
+// interior, 28-32 lose 2-7%).
 uint32_t walk_refill() {
   static uint32_t v = [] {
     const char* e = std::getenv("GBPT_WALK_REFILL");
-    int x = e ? std::atoi(e) : 24;
+    int x = e ? std::atoi(e) : 20;
     return (uint32_t)(x < 1 ? 1 : x > 32 ? 32 : x);
   }();
   return v;
@@ -880,11 +899,13 @@ cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream
 
 // Resident CTAs per SM the walk kernels are compiled for (register caps
 // 64 / 48 / 40 for k_walk, 128 / 80 for k_tail); GBPT_WALK_MINB /
-// GBPT_TAIL_MINB select a variant (tuning knobs; defaults from measurement).
+// GBPT_TAIL_MINB select a variant (tuning knobs).  Measured on the 1024x768
+// interior (depth 10) and the 1280x720 hall (depth 5): k_walk at 5 CTAs per
+// SM (48 registers) is 1-2% faster than 4 and 6; k_tail at 2 and 3 tie.
 int walk_minb() {
   static int v = [] {
     const char* e = std::getenv("GBPT_WALK_MINB");
-    int x = e ? std::atoi(e) : 4;
+    int x = e ? std::atoi(e) : 5;
     return x >= 6 ? 6 : x == 5 ? 5 : 4;
   }();
   return v;

@@ -60,6 +60,8 @@ struct FrameArgs {
   uint32_t cacheSel;    // light-vertex cache (0/1) this frame reads or the light pass writes
   uint32_t bilat;       // filter-only mode: direct-light sample, path potential, first-hit emissive
   uint32_t ptsc;        // unidirectional mode: no connections, total internal reflection reflects
+  uint32_t moments;     // learned allocator: per-pixel second moments and per-tile path-length counts
+  uint32_t tilesX;      // 8x8 tiles per image row
 };
 
 struct RenderBuffers {
@@ -71,6 +73,8 @@ struct RenderBuffers {
   float4* gbuf;         // per slot: 3 float4 (pos, normal, diffuse) when gbuffer; with bilat the
                         // three .w words hold the first-hit emissive
   float4* dsm;          // bilat, per slot: direct-light sample .xyz, path potential at termination .w
+  float* m2;            // moments: per-pixel running mean of (path sum)^2 / path count, RGB
+  uint32_t* hist;       // moments: per 8x8 tile, paths ended after 0..7+ surface hits (8 counts)
   uint32_t* slotPix;    // per slot pixel id
   uint32_t* slotSmp;    // per slot sample id
   float4* cache[2];     // two light-vertex caches (6 float4 per vertex): one is read by the
@@ -126,13 +130,29 @@ struct AdaptBuffers {
   double* partial;     // per reduce block
   float* filtered;     // W*H*3
   uint32_t* coop;      // binary allocator: barrier words, per-block counts, pass table
+  float* feat;         // learned allocator: 24 features per 8x8 tile
+  float* pred;         // learned allocator: log budget weight per tile
+  float* tileErr;      // learned allocator: sum of the heuristic error over each tile
 };
+constexpr uint32_t kFeatures = 24;
+constexpr uint32_t kErrMlpTimeout = 256u;  // DevCounters::errFlags bit: an MLP tensor-core wait ran out
 constexpr uint32_t kCoopWords = 8192;  // coop buffer size (uint32 words)
 cudaError_t launch_bilateral(const float* color, const float* pos, const float* norm, const float* emit, uint32_t W,
                              uint32_t H, float ceud, float peud, float neud, float eeud, uint32_t radius,
                              const float* g, float* out, cudaStream_t st);
 cudaError_t launch_adapt_budget(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab,
                                 const float* result, const uint32_t* sampleN, uint32_t desired, cudaStream_t st);
+// the two halves of launch_adapt_budget: per-pixel error (+ partial sums), then
+// sum, counts, offsets and camera paths from ab.err
+cudaError_t launch_adapt_error(const FrameArgs& a, const AdaptBuffers& ab, const float* result,
+                               const uint32_t* sampleN, uint32_t desired, cudaStream_t st);
+cudaError_t launch_adapt_alloc(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab, cudaStream_t st);
+// learned allocator: 24 features per 8x8 tile of the current statistics (needs ab.err)
+cudaError_t launch_tile_features(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab,
+                                 const float* result, const uint32_t* sampleN, const float* gpos, const float* gnorm,
+                                 const float* gdiff, cudaStream_t st);
+// learned allocator: per-pixel weights exp(pred[tile]) * err / tile sum; rewrites ab.err and its partial sums
+cudaError_t launch_mlp_alloc(const FrameArgs& a, const AdaptBuffers& ab, cudaStream_t st);
 cudaError_t launch_adapt_accum(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab, float* result,
                                uint32_t* sampleN, float* gpos, float* gnorm, float* gdiff, cudaStream_t st);
 // binary allocator (src/cudaRTBDPTStreamAdapBilatBinary.cu:1316-1418):

@@ -195,7 +195,9 @@ const float* gbpt_result(gbpt_renderer* r);
  * (W*H floats), 6 per-pixel sample count (W*H uint32), 7 light-vertex cache
  * (21 floats per vertex), and in BDPT_SC_BILAT: 8 direct-light running mean
  * RGB, 9 first-hit emissive RGB, 10 running mean of 1 - path potential
- * (W*H floats; the "Prob" debug view). */
+ * (W*H floats; the "Prob" debug view); with learned-allocator statistics on:
+ * 11 per-pixel second moments RGB, 12 per-tile path-length counts (8 uint32
+ * per 8x8 tile). */
 gbpt_status gbpt_read_buffer(gbpt_renderer* r, int32_t which, void* dst, size_t bytes, int32_t dst_is_device);
 /* Restart progressive accumulation (next frame is frame 0). */
 gbpt_status gbpt_reset(gbpt_renderer* r);
@@ -259,6 +261,46 @@ gbpt_status gbpt_renderer_rmse(gbpt_renderer* r, const float* converged, int32_t
  * be 4-byte aligned. */
 gbpt_status gbpt_tonemap_rgba8(const float* rgb, const float* ref, uint32_t width, uint32_t height, float exposure,
                                int32_t kind, uint8_t* out_rgba, int32_t is_device);
+
+/* ---- learned sample allocator (no reference counterpart: CudaPT links FANN
+ * but never calls it) -------------------------------------------------------
+ * A 24 -> 64 -> 64 -> 1 GELU MLP with BF16 weights and FP32 accumulation on
+ * the tensor cores (tcgen05), trained with Adam on mean squared error.
+ * Parameters: an FP32 vector of gbpt_mlp_param_count() = 5825 values laid out
+ * W1[64][24], b1[64], W2[64][64], b2[64], w3[64], b3.  Inputs: n rows of 24
+ * FP32 features; targets / outputs: n FP32 values. */
+typedef struct gbpt_mlp gbpt_mlp;
+uint32_t gbpt_mlp_param_count(void);
+/* He-uniform weights from Philox draws of `seed`, zero biases. */
+gbpt_status gbpt_mlp_create(uint32_t seed, gbpt_mlp** out);
+gbpt_status gbpt_mlp_destroy(gbpt_mlp* m);
+gbpt_status gbpt_mlp_get_params(gbpt_mlp* m, float* params);
+/* Also resets the Adam moments and step. */
+gbpt_status gbpt_mlp_set_params(gbpt_mlp* m, const float* params);
+gbpt_status gbpt_mlp_forward(gbpt_mlp* m, const float* x, uint32_t n, float* y, int32_t is_device);
+/* Gradient of mean((y - t)^2) (param_count values) and the loss; no update. */
+gbpt_status gbpt_mlp_gradients(gbpt_mlp* m, const float* x, const float* t, uint32_t n, int32_t is_device,
+                               float* grad, float* loss);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8, bias-corrected) on a batch. */
+gbpt_status gbpt_mlp_train_step(gbpt_mlp* m, const float* x, const float* t, uint32_t n, float lr,
+                                int32_t is_device, float* loss);
+
+/* Learned allocation in GBPT_MODE_BDPT_SC_ADAP_BILAT: with mlp != NULL every
+ * budgeted frame turns the heuristic per-pixel error into per-tile weights
+ * exp(mlp(features)) spread over each 8x8 tile in proportion to the heuristic
+ * (the network is not owned; keep it alive while attached).  collect != 0
+ * keeps the statistics the features need (per-pixel second moments, per-tile
+ * path-length counts) without changing the allocation.  NULL, 0: plain. */
+gbpt_status gbpt_renderer_set_mlp(gbpt_renderer* r, gbpt_mlp* mlp, int32_t collect);
+/* The 24 features of every 8x8 tile (row-major tiles, ceil(W/8) per row) of
+ * the current statistics (adaptive modes, after frames rendered with the
+ * statistics on): 0-2 log(1 + mean colour), 3-5 log(1 + 100 * mean variance of
+ * the pixel means), 6-8 mean albedo, 9-11 mean normal, 12 log(1 + mean
+ * first-hit distance), 13-20 fraction of paths ending after 0..7+ hits,
+ * 21 log2(1 + mean spp), 22/23 log(1 + 1000 * mean / max heuristic error).
+ * out == NULL: only *n_tiles. */
+gbpt_status gbpt_renderer_features(gbpt_renderer* r, float* out, uint32_t capacity, int32_t out_is_device,
+                                   uint32_t* n_tiles);
 
 /* ---- device math, exposed for verification -------------------------------
  * Evaluated by a kernel on host arrays x/out (copied in and out).

@@ -1,0 +1,115 @@
+"""Learned sample allocator in the renderer: tile targets on the CPU; on the
+GPU the feature kernel against a numpy restatement over the renderer's own
+planes, the statistics it reads (second moments, path-length counts), and
+learned allocation rendering the same image as the plain allocator."""
+import numpy as np
+import pytest
+
+from cudapt_gb300 import layouts, learned
+from helpers import scene_arrays
+
+
+def test_tile_targets():
+    W, H = 20, 12  # 3 x 2 tiles, ragged
+    ref = np.zeros(W * H * 3, np.float32)
+    img = ref.copy().reshape(H, W, 3)
+    img[:8, :8] = 1.0      # tile 0: mse 1
+    img[:8, 8:16] = 0.5    # tile 1: mse 0.25
+    img[8:, 16:] = 2.0     # tile 5 (4 x 4 pixels): mse 4
+    t = learned.tile_targets(img.reshape(-1), ref, W, H)
+    raw = 0.5 * np.log(np.array([1.0, 0.25, 0, 0, 0, 4.0]) + learned.EPS)
+    np.testing.assert_allclose(t, raw - raw.mean(), rtol=1e-6, atol=1e-6)
+    assert abs(t.mean()) < 1e-6
+
+
+def _numpy_features(r, cam, err):
+    W, H = r.width, r.height
+    res = r.read_buffer(0).reshape(H, W, 3).astype(np.float64)
+    n = r.read_buffer(6).reshape(H, W).astype(np.float64)
+    m2 = r.read_buffer(11).reshape(H, W, 3).astype(np.float64)
+    pos, nrm, dif = (r.read_buffer(k).reshape(H, W, 3).astype(np.float64) for k in (1, 2, 3))
+    hist = r.read_buffer(12).reshape(-1, 8).astype(np.float64)
+    e = err.reshape(H, W).astype(np.float64)
+    tx, ty = (W + 7) // 8, (H + 7) // 8
+    out = np.zeros((tx * ty, 24))
+    cp = np.array(cam["pos"], np.float64)
+    for j in range(ty):
+        for i in range(tx):
+            sl = (slice(j * 8, min(j * 8 + 8, H)), slice(i * 8, min(i * 8 + 8, W)))
+            mu = res[sl]
+            var = np.where(n[sl][..., None] > 0, np.maximum(m2[sl] - mu * mu, 0) / np.maximum(n[sl][..., None], 1), 0)
+            f = out[j * tx + i]
+            f[0:3] = np.log1p(np.maximum(mu.reshape(-1, 3).mean(0), 0))
+            f[3:6] = np.log1p(100 * var.reshape(-1, 3).mean(0))
+            f[6:9] = dif[sl].reshape(-1, 3).mean(0)
+            f[9:12] = nrm[sl].reshape(-1, 3).mean(0)
+            f[12] = np.log1p(np.linalg.norm(pos[sl] - cp, axis=-1).mean())
+            h = hist[j * tx + i]
+            f[13:21] = h / h.sum() if h.sum() > 0 else 0
+            f[21] = np.log2(1 + n[sl].mean())
+            f[22] = np.log1p(1000 * e[sl].mean())
+            f[23] = np.log1p(1000 * e[sl].max())
+    return out
+
+
+@pytest.mark.gpu
+def test_gpu_features_match_numpy(gbdev):
+    (v, t, m), cam = scene_arrays("cornell")
+    W, H = 52, 36  # ragged tiles on both axes
+    s = gbdev.RTScene(v, t, m).build_bvh()
+    r = gbdev.RTRenderer(W, H, layouts.MODE_BDPT_SC_ADAP_BILAT,
+                         learned.adaptive_params(8, warmup_frames=2, filter_radius=3))
+    r.set_mlp(None, collect=True)
+    for _ in range(4):
+        r.render(s, cam)
+    f = r.features()
+    assert f.shape == (7 * 5, 24)
+    hist = r.read_buffer(12)
+    # every camera path of the 4 frames ended exactly once (2 uniform frames of W*H paths + 2 budgeted)
+    assert hist.sum() == 4 * W * H
+    m2, mu = r.read_buffer(11), r.read_buffer(0)
+    assert np.all(m2 >= mu * mu * (1 - 1e-5) - 1e-7)  # E[x^2] >= E[x]^2
+    want = _numpy_features(r, cam, r.read_buffer(5))
+    np.testing.assert_allclose(f, want, rtol=2e-4, atol=2e-5)
+
+
+@pytest.mark.gpu
+def test_gpu_learned_allocation_renders_same_image(gbdev):
+    """A (random) network changes where samples go, not what converges: the
+    learned and plain allocators agree within Monte Carlo noise."""
+    from cudapt_gb300.mlp import MLP
+    (v, t, m), cam = scene_arrays("cornell")
+    W, H = 48, 48
+    s = gbdev.RTScene(v, t, m).build_bvh()
+    p = learned.adaptive_params(8, warmup_frames=2, filter_radius=3)
+    net = MLP(seed=3)
+    imgs, counts = [], []
+    for mlp in (None, net):
+        r = gbdev.RTRenderer(W, H, layouts.MODE_BDPT_SC_ADAP_BILAT, p)
+        r.set_mlp(mlp)
+        for _ in range(40):
+            img = r.render(s, cam)
+        imgs.append(img.copy())
+        counts.append(r.read_buffer(6).copy())
+        assert r.last_stats["paths"] <= W * H
+    assert not np.array_equal(counts[0], counts[1])  # the allocation differs
+    a, b = (x.reshape(H, W, 3)[:, :, :].reshape(6, 8, 6, 8, 3).mean(axis=(1, 3)) for x in imgs)
+    assert abs(a.mean() - b.mean()) <= 0.05 * a.mean()
+    np.testing.assert_allclose(a, b, rtol=0.25, atol=0.02)
+
+
+@pytest.mark.gpu
+def test_gpu_training_on_rendered_tiles(gbdev):
+    """Samples from two small hall scenes: the trained network predicts the
+    held-out scene's tile errors better than a constant."""
+    Xs, Ys = [], []
+    for seed in (1, 2, 21):
+        X, Y = learned.samples_for_scene(gbdev, seed, width=128, height=72, snapshots=(5, 8), conv_frames=128,
+                                         boxes=60)
+        Xs.append(X)
+        Ys.append(Y)
+    net, losses = learned.train(np.concatenate(Xs[:2]), np.concatenate(Ys[:2]), steps=300, batch=1024, lr=3e-3)
+    assert losses[-20:].mean() < 0.7 * losses[:5].mean()
+    pred = net.forward(Xs[2])
+    pred -= pred.mean()
+    assert np.mean((pred - Ys[2]) ** 2) < 0.9 * np.mean(Ys[2] ** 2)

@@ -269,12 +269,30 @@ def bench_gpu(args):
                      "frac": round(achieved / peak, 4) if achieved else None, "peak_kind": peak_kind,
                      "traffic": traffic,
                      "algorithmic_bytes_per_frame": int(trace_bytes)},
+        "filter_roofline": filter_roofline(phases, args.steps, np_, peak) if WL[3] == 1 else None,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": launches,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def filter_roofline(phases, steps, np_, peak):
+    """Bilateral filter of a budgeted frame against its compulsory traffic: the colour,
+    position and normal planes read (12 B per pixel each) and 12 B per pixel written."""
+    ms = phases["ms_filter"] / steps
+    if ms <= 0:
+        return None
+    planes = 3
+    compulsory = (planes * 12 + 12) * np_
+    radius = 4
+    gbs = compulsory / (ms / 1e3) / 1e9
+    return {"kernel": "k_bilateral_tile", "bound": "hbm", "ms_per_frame": round(ms, 4),
+            "compulsory_bytes": compulsory, "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(gbs / peak, 4),
+            "taps_per_pixel": (2 * radius + 1) ** 2,
+            "algorithmic_bytes_naive": (2 * radius + 1) ** 2 * planes * 12 * np_}
 
 
 def profiled_traffic(workload):

@@ -100,6 +100,7 @@ SIGNATURES = {
     "gbpt_mlp_forward": (i32, [vp, vp, u32, vp, i32]),
     "gbpt_mlp_gradients": (i32, [vp, vp, vp, u32, i32, vp, vp]),
     "gbpt_mlp_train_step": (i32, [vp, vp, vp, u32, f32, i32, vp]),
+    "gbpt_renderer_set_stream": (i32, [vp, vp]),
     "gbpt_renderer_set_mlp": (i32, [vp, vp, i32]),
     "gbpt_renderer_features": (i32, [vp, vp, u32, i32, vp]),
     "gbpt_fmath": (i32, [i32, vp, u32, vp]),

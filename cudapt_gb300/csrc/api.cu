@@ -188,6 +188,9 @@ struct gbpt_renderer {
   // learned allocator: the attached network (not owned), whether statistics are kept without one
   gbpt_mlp* mlp = nullptr;
   bool collect = false;
+  // work stream: the renderer's own (ownSt) unless the caller supplied one
+  bool userStream = false;
+  cudaStream_t ownSt = nullptr;
   const float* bilatOut = nullptr;  // filter plane holding the last filtered image
   uint32_t* sampleN = nullptr;
   float4* waveMem = nullptr;
@@ -261,7 +264,8 @@ struct gbpt_renderer {
     for (cudaEvent_t e : {evMain, evLight[0], evLight[1]})
       if (e) cudaEventDestroy(e);
     if (stLight) cudaStreamDestroy(stLight);
-    if (st) cudaStreamDestroy(st);
+    if (st && !userStream) cudaStreamDestroy(st);
+    if (ownSt && ownSt != st) cudaStreamDestroy(ownSt);
   }
 };
 
@@ -1013,7 +1017,9 @@ gbpt_status gbpt_render_frames(gbpt_renderer* r, gbpt_scene* s, const gbpt_camer
 
 const float* gbpt_result(gbpt_renderer* r) {
   if (!r || !r->alloc) return nullptr;
-  if (cudaMemcpy(r->hostResult.data(), r->result, r->hostResult.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+  // the image gbpt_render copies out (the mode's current view), as the reference's GetResult returns
+  if (cudaStreamSynchronize(r->st) != cudaSuccess ||
+      cudaMemcpy(r->hostResult.data(), output_view(r), r->hostResult.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
     return nullptr;
   return r->hostResult.data();
 }
@@ -1084,6 +1090,15 @@ gbpt_status gbpt_renderer_rmse(gbpt_renderer* r, const float* converged, int32_t
   cudaStreamSynchronize(r->st);
   dfree(d);
   return st;
+}
+
+gbpt_status gbpt_renderer_set_stream(gbpt_renderer* r, void* stream) {
+  if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
+  CK(cudaStreamSynchronize(r->st));
+  if (!r->ownSt) r->ownSt = r->st;
+  r->st = stream ? (cudaStream_t)stream : r->ownSt;
+  r->userStream = stream != nullptr;
+  return GBPT_OK;
 }
 
 gbpt_status gbpt_renderer_set_mlp(gbpt_renderer* r, gbpt_mlp* mlp, int32_t collect) {

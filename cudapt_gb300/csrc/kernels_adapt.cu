@@ -305,6 +305,7 @@ __device__ __forceinline__ float bfly(float v) {
   return v;
 }
 
+template <bool kMoments>
 __global__ void k_accum(FrameArgs a, RenderBuffers b, const uint32_t* __restrict__ off,
                         const uint32_t* __restrict__ cnt, float* result, uint32_t* sampleN, float* gpos,
                         float* gnorm, float* gdiff) {
@@ -325,12 +326,12 @@ __global__ void k_accum(FrameArgs a, RenderBuffers b, const uint32_t* __restrict
     v[3] = v[3] + g0.x * fn; v[4] = v[4] + g0.y * fn; v[5] = v[5] + g0.z * fn;
     v[6] = v[6] + g1.x * fn; v[7] = v[7] + g1.y * fn; v[8] = v[8] + g1.z * fn;
     v[9] = v[9] + g2.x * fn; v[10] = v[10] + g2.y * fn; v[11] = v[11] + g2.z * fn;
-    if (a.moments) {  // second moments for the learned allocator's features
+    if (kMoments) {  // second moments for the learned allocator's features
       v[12] = v[12] + (r.x * r.x) / fn; v[13] = v[13] + (r.y * r.y) / fn; v[14] = v[14] + (r.z * r.z) / fn;
     }
     tN += n;
   }
-  for (int k = 0; k < (a.moments ? 15 : 12); k++) v[k] = bfly(v[k]);
+  for (int k = 0; k < (kMoments ? 15 : 12); k++) v[k] = bfly(v[k]);
   for (int m = 16; m > 0; m >>= 1) tN += __shfl_xor_sync(0xffffffffu, tN, m);
   if (lane != 0) return;
   float* q = result + 3 * (size_t)p;
@@ -345,7 +346,7 @@ __global__ void k_accum(FrameArgs a, RenderBuffers b, const uint32_t* __restrict
   const uint32_t nn = tN + N;
   if (nn > N) {
     const float rInf = 1.f / (float)nn, oInf = (float)N * rInf;
-    if (a.moments) {
+    if (kMoments) {
       float* m = b.m2 + 3 * (size_t)p;
       for (int k = 0; k < 3; k++) m[k] = N ? rInf * v[12 + k] + oInf * m[k] : rInf * v[12 + k];
     }
@@ -729,8 +730,12 @@ __global__ void k_tile_features(FrameArgs a, RenderBuffers b, AdaptBuffers ab, c
   f[13 + lane] = hsum ? (float)hp[lane] / (float)hsum : 0.f;
 }
 
-// e'_p = exp(pred[tile]) * e_p / (sum of e over the tile), or exp(pred) / pixels
-// when the tile's heuristic error is zero; FP64 partial sums as k_error's
+// The network predicts pred = 1/2 log(MSE_t) of the tile's current image
+// (up to a constant); one more sample per pixel lowers the tile's error
+// V_t / n by about V_t / n^2 = MSE_t / n, so the tile's weight this frame is
+// w = exp(2 pred) / n (n: the tile's mean samples per pixel, from feature 21).
+// e'_p = w * e_p / (sum of e over the tile), or w / pixels when the tile's
+// heuristic error is zero; FP64 partial sums as k_error's.
 __global__ void __launch_bounds__(kReduceBlock) k_mlp_alloc(FrameArgs a, AdaptBuffers ab, uint32_t np) {
   __shared__ double ws[kReduceBlock / 32];
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -738,7 +743,8 @@ __global__ void __launch_bounds__(kReduceBlock) k_mlp_alloc(FrameArgs a, AdaptBu
   if (p < np) {
     const uint32_t x = p % a.width, y = p / a.width;
     const uint32_t tile = (y >> 3) * a.tilesX + (x >> 3);
-    const float w = expf(fminf(fmaxf(ab.pred[tile], -30.f), 30.f));
+    const float nMean = exp2f(ab.feat[(size_t)tile * kFeatures + 21]) - 1.f;
+    const float w = expf(fminf(fmaxf(2.f * ab.pred[tile], -60.f), 60.f)) / fmaxf(nMean, 1.f);
     const float S = ab.tileErr[tile];
     const uint32_t tw = min(8u, a.width - (x & ~7u)), th = min(8u, a.height - (y & ~7u));
     const float e = S > 0.f ? w * (ab.err[p] / S) : w / (float)(tw * th);
@@ -774,8 +780,11 @@ cudaError_t launch_mlp_alloc(const FrameArgs& a, const AdaptBuffers& ab, cudaStr
 cudaError_t launch_adapt_accum(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab, float* result,
                                uint32_t* sampleN, float* gpos, float* gnorm, float* gdiff, cudaStream_t st) {
   const uint32_t np = a.width * a.height;
-  k_accum<<<(uint32_t)(((size_t)np * 32 + 255) / 256), 256, 0, st>>>(a, b, ab.off, ab.cnt, result, sampleN, gpos,
-                                                                     gnorm, gdiff);
+  const uint32_t g = (uint32_t)(((size_t)np * 32 + 255) / 256);
+  if (a.moments)
+    k_accum<true><<<g, 256, 0, st>>>(a, b, ab.off, ab.cnt, result, sampleN, gpos, gnorm, gdiff);
+  else
+    k_accum<false><<<g, 256, 0, st>>>(a, b, ab.off, ab.cnt, result, sampleN, gpos, gnorm, gdiff);
   note_launches(1);
   return cudaGetLastError();
 }

@@ -859,9 +859,9 @@ uint32_t walk_refill() {
   return v;
 }
 
-uint32_t grid_for(const void* kernel) {
+uint32_t grid_for(const void* kernel, size_t smem = 0) {
   int per = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kBlock, smem);
   if (per < 1) per = 1;
   return (uint32_t)(sm_count() * per);
 }

@@ -1,16 +1,19 @@
 """Training and evaluation of the learned sample allocator.
 
 The network (cudapt_gb300.mlp, kernels in csrc/mlp.cu) maps the 24 features
-of an 8x8 tile (``gbpt_renderer_features``) to a log budget weight; the PLL
-adaptive mode spends samples in proportion to exp(weight), spread inside the
+of an 8x8 tile (``gbpt_renderer_features``) to pred = 1/2 log of the tile's
+current mean squared error (up to a per-image constant); the PLL adaptive
+mode then gives each tile a share of the frame's samples proportional to
+exp(2 pred) / n_t (n_t: the tile's mean samples per pixel), spread inside the
 tile by the plain heuristic (``gbpt_renderer_set_mlp``).
 
-Targets.  With n_t samples per pixel in tile t and per-pixel variances v_p,
-the tile's summed squared error is V_t / n_t (V_t = sum of v_p over the tile);
-for a fixed total budget, sum_t V_t / n_t is smallest at n_t proportional to
-sqrt(V_t).  The squared error of a low-sample image against a converged one
-estimates V_t / n, so the target is 0.5 log(tile mean squared error),
-centred per image (only ratios of budgets matter).
+Why.  With n_t samples per pixel and per-pixel variances summing to V_t over
+the tile, the tile's squared error is V_t / n_t; one more sample per pixel
+lowers it by about V_t / n_t^2 = MSE_t / n_t, and spending each frame where
+that gain is largest drives the allocation towards the fixed-budget optimum
+n_t proportional to sqrt(V_t) while accounting for samples already spent.
+The squared error of the current image against a converged one estimates
+MSE_t, so the training target is 0.5 log(tile MSE), centred per image.
 
 Protocol (the benchmark's learned-sampler configuration): hall scenes of the
 procedural generator, seeds 1-20 for training and 21-25 held out; features
@@ -95,7 +98,7 @@ def train(X, Y, steps=2000, batch=4096, lr=1e-3, seed=0, log_every=0):
 
 def equal_time(gb, seed, net, seconds, width=320, height=180, ref=None, conv_frames=1024, boxes=300):
     """RMSE against the reference after `seconds` of rendering, plain vs learned allocation.
-    Returns dict(plain=(rmse, frames), learned=(rmse, frames))."""
+    Returns dict(plain=(rmse, frames, image), learned=(rmse, frames, image))."""
     (v, t, m), cam = hall_scene(seed, boxes)
     scene = gb.RTScene(v, t, m).build_bvh()
     if ref is None:
@@ -112,6 +115,6 @@ def equal_time(gb, seed, net, seconds, width=320, height=180, ref=None, conv_fra
             r.render(scene, cam, stats=False)
             elapsed += time.perf_counter() - t0
             frames += 1
-        out[name] = (r.rmse(ref), frames)
+        out[name] = (r.rmse(ref), frames, r.GetResult().copy())
         r.close()
     return out

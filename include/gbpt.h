@@ -285,6 +285,11 @@ gbpt_status gbpt_mlp_gradients(gbpt_mlp* m, const float* x, const float* t, uint
 gbpt_status gbpt_mlp_train_step(gbpt_mlp* m, const float* x, const float* t, uint32_t n, float lr,
                                 int32_t is_device, float* loss);
 
+/* Run the renderer's work on the caller's cudaStream_t (NULL: back to its own
+ * stream), so that several renderers can be batched on streams the caller
+ * schedules.  Every call still returns when its frame is complete. */
+gbpt_status gbpt_renderer_set_stream(gbpt_renderer* r, void* stream);
+
 /* Learned allocation in GBPT_MODE_BDPT_SC_ADAP_BILAT: with mlp != NULL every
  * budgeted frame turns the heuristic per-pixel error into per-tile weights
  * exp(mlp(features)) spread over each 8x8 tile in proportion to the heuristic

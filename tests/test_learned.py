@@ -60,13 +60,15 @@ def test_gpu_features_match_numpy(gbdev):
     r = gbdev.RTRenderer(W, H, layouts.MODE_BDPT_SC_ADAP_BILAT,
                          learned.adaptive_params(8, warmup_frames=2, filter_radius=3))
     r.set_mlp(None, collect=True)
+    paths = 0
     for _ in range(4):
         r.render(s, cam)
+        paths += r.last_stats["paths"]
     f = r.features()
     assert f.shape == (7 * 5, 24)
     hist = r.read_buffer(12)
-    # every camera path of the 4 frames ended exactly once (2 uniform frames of W*H paths + 2 budgeted)
-    assert hist.sum() == 4 * W * H
+    # every camera path of the 4 frames (2 uniform frames of W*H, 2 budgeted) ended exactly once
+    assert hist.sum() == paths and paths > 2 * W * H
     m2, mu = r.read_buffer(11), r.read_buffer(0)
     assert np.all(m2 >= mu * mu * (1 - 1e-5) - 1e-7)  # E[x^2] >= E[x]^2
     want = _numpy_features(r, cam, r.read_buffer(5))
@@ -75,27 +77,34 @@ def test_gpu_features_match_numpy(gbdev):
 
 @pytest.mark.gpu
 def test_gpu_learned_allocation_renders_same_image(gbdev):
-    """A (random) network changes where samples go, not what converges: the
-    learned and plain allocators agree within Monte Carlo noise."""
+    """The network changes where samples go, not what converges: images of
+    the plain allocator, of a network whose output is constant (equal budget
+    per tile) and of a random network all approach the same long plain
+    render, with errors of the same size."""
     from cudapt_gb300.mlp import MLP
+    from oracle import mlp_ref
     (v, t, m), cam = scene_arrays("cornell")
     W, H = 48, 48
     s = gbdev.RTScene(v, t, m).build_bvh()
     p = learned.adaptive_params(8, warmup_frames=2, filter_radius=3)
-    net = MLP(seed=3)
-    imgs, counts = [], []
-    for mlp in (None, net):
+    ref = learned.converged(gbdev, s, cam, W, H, 2048, depth=8)
+    flat = mlp_ref.init(4)
+    flat[-65:] = 0.0  # w3 = 0, b3 = 0: every tile gets weight exp(0)
+    nets = {"plain": None, "flat": MLP(params=flat.astype(np.float32)), "random": MLP(seed=3)}
+    err, counts = {}, {}
+    for name, mlp in nets.items():
         r = gbdev.RTRenderer(W, H, layouts.MODE_BDPT_SC_ADAP_BILAT, p)
         r.set_mlp(mlp)
         for _ in range(40):
             img = r.render(s, cam)
-        imgs.append(img.copy())
-        counts.append(r.read_buffer(6).copy())
-        assert r.last_stats["paths"] <= W * H
-    assert not np.array_equal(counts[0], counts[1])  # the allocation differs
-    a, b = (x.reshape(H, W, 3)[:, :, :].reshape(6, 8, 6, 8, 3).mean(axis=(1, 3)) for x in imgs)
-    assert abs(a.mean() - b.mean()) <= 0.05 * a.mean()
-    np.testing.assert_allclose(a, b, rtol=0.25, atol=0.02)
+            assert r.last_stats["paths"] <= W * H
+        counts[name] = r.read_buffer(6).copy()
+        err[name] = float(np.sqrt(np.mean((img.astype(np.float64) - ref) ** 2)))
+        assert abs(img.mean() - ref.mean()) <= 0.08 * ref.mean(), (name, img.mean(), ref.mean())
+    assert not np.array_equal(counts["plain"], counts["random"])  # the allocation differs
+    assert not np.array_equal(counts["plain"], counts["flat"])
+    for name in ("flat", "random"):
+        assert err[name] <= 2.5 * err["plain"], err
 
 
 @pytest.mark.gpu

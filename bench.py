@@ -193,6 +193,8 @@ def bench_gpu(args):
     (v, t, m), cam = scene_and_camera()
     scene = gb.RTScene(v, t, m).build_bvh()
     build_s = scene.build_seconds
+    if args.traversal == "wide":
+        scene.set_traversal("wide")
     params = params_for(gb)
     np_ = W * H
     r = gb.RTRenderer(W, H, WL[3], params)
@@ -235,7 +237,10 @@ def bench_gpu(args):
     r.set_counting(True)
     cst = r.render_frames(scene, cam, 1, stats=True)
     r.set_counting(False)
-    trace_bytes = 40 * (cst["nodes"] + cst["shadow_nodes"]) + 48 * (cst["tris"] + cst["shadow_tris"])
+    # bytes per visited node: 32 B bounds + 8 B child words (reference order); 112 B per
+    # wide node (4 boxes + 4 child codes); 48 B per triangle test
+    node_bytes = 112 if args.traversal == "wide" else 40
+    trace_bytes = node_bytes * (cst["nodes"] + cst["shadow_nodes"]) + 48 * (cst["tris"] + cst["shadow_tris"])
     trace_ms = cst["ms_trace"]
     achieved = trace_bytes / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else None
     peak, peak_kind = load_peaks()
@@ -260,6 +265,7 @@ def bench_gpu(args):
                    "eye_depth_max": D, "light_depth_max": D, "tris": int(len(t)),
                    "l2": "flushed before every timed step (256 MB device memset)",
                    "bvh_build_s": round(build_s, 4), "rays_per_s": round(rays / (total_ms / 1e3), 1),
+                   "traversal": args.traversal,
                    "phase_ms_per_step": {k: round(v_ / args.steps, 4) for k, v_ in phases.items()},
                    "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": round(e2e * world, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": 40,
@@ -270,6 +276,7 @@ def bench_gpu(args):
                      "traffic": traffic,
                      "algorithmic_bytes_per_frame": int(trace_bytes)},
         "filter_roofline": filter_roofline(phases, args.steps, np_, peak) if WL[3] == 1 else None,
+        "learned_sampler": learned_sampler_summary(),
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": launches,
@@ -293,6 +300,22 @@ def filter_roofline(phases, steps, np_, peak):
             "frac": round(gbs / peak, 4),
             "taps_per_pixel": (2 * radius + 1) ** 2,
             "algorithmic_bytes_naive": (2 * radius + 1) ** 2 * planes * 12 * np_}
+
+
+def learned_sampler_summary():
+    """Equal-time RMSE of the learned allocator over the plain PLL allocator (held-out hall
+    scenes), from the committed report of tests/experiments/learned_sampler.py."""
+    p = os.path.join(ROOT, "profiles", "learned_sampler_hall_320x180.md")
+    if not os.path.exists(p):
+        return None
+    out = {"report": "profiles/learned_sampler_hall_320x180.md", "scenes": "hall seeds 21-25, 320x180",
+           "equal_time_s": [0.25, 0.5, 1.0]}
+    with open(p) as f:
+        for ln in f:
+            parts = ln.split()
+            if len(parts) == 2 and parts[0].startswith("learned_over_plain_rmse_"):
+                out[parts[0]] = float(parts[1])
+    return out
 
 
 def profiled_traffic(workload):
@@ -331,6 +354,8 @@ def main():
     ap.add_argument("--impl", default="gbpt", choices=["gbpt", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="interior", choices=sorted(WORKLOADS))
+    ap.add_argument("--traversal", default="reference", choices=["reference", "wide"],
+                    help="BVH walk order: the reference's (bit-exact, default) or the collapsed 4-wide tree")
     args = ap.parse_args()
     global WL, WORKLOAD, W, H
     WL = WORKLOADS[args.workload]

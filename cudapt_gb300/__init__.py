@@ -78,6 +78,13 @@ class RTScene:
         self.materials = as_c(materials, MATERIAL)
         check(load().gbpt_scene_update_materials(self._h, ptr(self.materials), len(self.materials)))
 
+    def set_traversal(self, mode):
+        """BVH walk order: 0 / "reference" (bit-exact with TracePrimitive, the default) or
+        1 / "wide" (collapsed 4-ary tree, nearest child first; same closest hits)."""
+        m = {"reference": 0, "wide": 1}.get(mode, mode)
+        check(load().gbpt_scene_set_traversal(self._h, int(m)))
+        return self
+
     def bvh_info(self):
         n, t, l = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
         check(load().gbpt_scene_bvh_info(self._h, ctypes.addressof(n), ctypes.addressof(t), ctypes.addressof(l)))

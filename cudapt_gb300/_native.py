@@ -67,6 +67,7 @@ SIGNATURES = {
     "gbpt_scene_destroy": (i32, [vp]),
     "gbpt_scene_build_bvh": (i32, [vp, u32, u32, vp]),
     "gbpt_scene_update_materials": (i32, [vp, vp, u32]),
+    "gbpt_scene_set_traversal": (i32, [vp, i32]),
     "gbpt_scene_bvh_info": (i32, [vp, vp, vp, vp]),
     "gbpt_scene_bvh_export": (i32, [vp, vp, vp, vp]),
     "gbpt_trace_rays": (i32, [vp, vp, u32, f32, f32, i32, vp, vp, vp, vp, vp, vp, vp, i32]),

@@ -70,7 +70,8 @@ struct gbpt_scene {
   bool built = false;
   std::vector<gbpt_triangle> trisOrdered;
   std::vector<uint32_t> lightTri;
-  float4 *dNodes = nullptr, *dTris = nullptr, *dShade = nullptr, *dMats = nullptr;
+  float4 *dNodes = nullptr, *dTris = nullptr, *dShade = nullptr, *dMats = nullptr, *dWide = nullptr;
+  uint32_t traversal = 0;  // 0: the reference's order, 1: wide (collapsed 4-ary tree)
   uint32_t* dLight = nullptr;
   DevScene dev;
   uint64_t version = 0;
@@ -82,6 +83,7 @@ struct gbpt_scene {
     dfree(dShade);
     dfree(dMats);
     dfree(dLight);
+    dfree(dWide);
     dev = DevScene{};
   }
   ~gbpt_scene() { free_dev(); }
@@ -113,6 +115,16 @@ float as_f(uint32_t u) {
   float f;
   std::memcpy(&f, &u, 4);
   return f;
+}
+
+gbpt_status upload_wide(gbpt_scene* s) {
+  dfree(s->dWide);
+  std::vector<float> w = collapse_wide(s->bvh);
+  CK(dalloc(&s->dWide, w.size() / 4));
+  CK(cudaMemcpy(s->dWide, w.data(), w.size() * 4, cudaMemcpyHostToDevice));
+  s->dev.wide = s->dWide;
+  s->dev.wideN = (uint32_t)(w.size() / 32);
+  return GBPT_OK;
 }
 
 gbpt_status upload_scene(gbpt_scene* s) {
@@ -158,6 +170,11 @@ gbpt_status upload_scene(gbpt_scene* s) {
   s->dev.triN = nt;
   s->dev.lightN = (uint32_t)s->lightTri.size();
   s->dev.matN = (uint32_t)s->mats.size();
+  s->dev.traversal = s->traversal;
+  if (s->traversal == 1) {
+    gbpt_status w = upload_wide(s);
+    if (w != GBPT_OK) return w;
+  }
   s->uploaded = true;
   return GBPT_OK;
 }
@@ -846,6 +863,21 @@ gbpt_status gbpt_scene_build_bvh(gbpt_scene* s, uint32_t max_depth, uint32_t thr
   s->uploaded = false;
   s->built = true;
   s->version = next_version();
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_scene_set_traversal(gbpt_scene* s, int32_t traversal) {
+  if (!s) return fail(GBPT_ERR_INVALID_ARG, "scene is NULL");
+  if (traversal != 0 && traversal != 1) return fail(GBPT_ERR_INVALID_ARG, "traversal is 0 (reference) or 1 (wide)");
+  if ((uint32_t)traversal == s->traversal) return GBPT_OK;
+  s->traversal = (uint32_t)traversal;
+  s->version = next_version();  // progressive accumulation restarts
+  if (!s->uploaded) return GBPT_OK;
+  if (traversal == 1 && !s->dWide) {
+    gbpt_status w = upload_wide(s);
+    if (w != GBPT_OK) return w;
+  }
+  s->dev.traversal = s->traversal;
   return GBPT_OK;
 }
 

@@ -19,6 +19,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <memory>
 #include <thread>
 #include <vector>
@@ -228,6 +229,75 @@ bool build_bvh(const gbpt_vertex* verts, const gbpt_triangle* tris, uint32_t nt,
   out->offOrTSTN.assign((size_t)out->nodeN * 2, 0u);
   out->emptyChildren = c.emptyChildren.load();
   return compact(&root, *out, 0) == out->nodeN;
+}
+
+std::vector<float> collapse_wide(const HostBVH& bvh) {
+  constexpr uint32_t kEmpty = 0xFFFFFFFFu, kLeaf = 0x80000000u, kTri = 0xC0000000u;
+  const uint32_t n = bvh.nodeN;
+  auto emptyBox = [&](uint32_t i) { return bvh.bounds[6 * (size_t)i] > bvh.bounds[6 * (size_t)i + 3]; };
+  // an inner node has a zero triangle count and a non-empty box (an empty leaf
+  // also stores a zero count, but its box is empty)
+  auto inner = [&](uint32_t i) { return bvh.offOrTSTN[2 * (size_t)i + 1] == 0 && !emptyBox(i); };
+  std::vector<float> out;
+  std::vector<uint32_t> src;  // binary node each wide node was made from
+  auto add = [&](uint32_t b) {
+    src.push_back(b);
+    out.resize(out.size() + 32, 0.f);
+    return (uint32_t)(src.size() - 1);
+  };
+  if (n == 0) return out;
+  add(0);
+  for (size_t w = 0; w < src.size(); w++) {
+    const uint32_t b = src[w];
+    uint32_t slot[4], ns = 0;
+    if (!inner(b)) {
+      slot[ns++] = b;  // a leaf root
+    } else {
+      const uint32_t kids[2] = {b + 1, b + bvh.offOrTSTN[2 * (size_t)b]};
+      for (uint32_t c : kids) {
+        if (c >= n) continue;
+        if (inner(c)) {
+          slot[ns++] = c + 1;
+          slot[ns++] = c + bvh.offOrTSTN[2 * (size_t)c];
+        } else {
+          slot[ns++] = c;
+        }
+      }
+    }
+    float lo[3][4], hi[3][4];
+    uint32_t code[4];
+    for (int k = 0; k < 4; k++) {
+      code[k] = kEmpty;
+      for (int a = 0; a < 3; a++) {
+        lo[a][k] = 1e20f;
+        hi[a][k] = -1e20f;
+      }
+    }
+    for (uint32_t k = 0; k < ns; k++) {
+      const uint32_t s = slot[k];
+      if (s >= n || emptyBox(s)) continue;
+      for (int a = 0; a < 3; a++) {
+        lo[a][k] = bvh.bounds[6 * (size_t)s + a];
+        hi[a][k] = bvh.bounds[6 * (size_t)s + 3 + a];
+      }
+      const uint32_t tn = bvh.offOrTSTN[2 * (size_t)s + 1];
+      if (inner(s))
+        code[k] = add(s);
+      else if (tn == 1)
+        code[k] = kTri | bvh.offOrTSTN[2 * (size_t)s];
+      else
+        code[k] = kLeaf | s;
+    }
+    float* r = &out[w * 32];
+    for (int k = 0; k < 4; k++) {
+      for (int a = 0; a < 3; a++) {
+        r[a * 4 + k] = lo[a][k];
+        r[12 + a * 4 + k] = hi[a][k];
+      }
+      std::memcpy(&r[24 + k], &code[k], 4);
+    }
+  }
+  return out;
 }
 
 }  // namespace gbpt

@@ -20,6 +20,11 @@ struct HostBVH {
 bool build_bvh(const gbpt_vertex* verts, const gbpt_triangle* tris, uint32_t nt, uint32_t maxDepth, uint32_t threads,
                HostBVH* out);
 
+// The binary tree collapsed to 4-wide nodes for the wide traversal: 32 floats
+// per node (lo.x[4], lo.y[4], lo.z[4], hi.x[4], hi.y[4], hi.z[4], code[4] as
+// uint bits, 4 zeros); see DevScene in launch.h for the child codes.
+std::vector<float> collapse_wide(const HostBVH& bvh);
+
 // sqrt(mean((a - b)^2)) over n floats in device memory, summed in double on
 // `stream` (a cudaStream_t); image.cu
 gbpt_status rmse_device(const float* a, const float* b, uint64_t n, double* out, void* stream);

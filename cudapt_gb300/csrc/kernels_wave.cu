@@ -369,9 +369,12 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, uint32_t v
 // results do not depend on this scheduling.  The any-hit walk stops at the
 // first hit closer than maxDist: that is exactly when the reference's
 // closest-hit walk with the same maxDist would report a hit.
-template <bool kCount, int kMinBlocks>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_walk(DevScene S, RenderBuffers b, int in, int shIn, int shReset,
-                                                 uint32_t shDirect, uint32_t kRefill) {
+// 5 resident CTAs per SM (48 registers) for the reference order: measured
+// 1-2% faster than 4 or 6 on the interior and hall workloads; 4 for the wide
+// walk (its wide-node step needs more registers).
+template <bool kCount, bool kWide>
+__global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, RenderBuffers b, int in, int shIn,
+                                                              int shReset, uint32_t shDirect, uint32_t kRefill) {
   const uint32_t nE = (in >= 0) ? b.ctr->wave[in] : 0u;
   const uint32_t nS = (shIn >= 0) ? b.ctr->shadow[shIn] : 0u;
   const uint32_t n = nE + nS;
@@ -385,8 +388,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_walk(DevScene S, RenderB
   const Wave wv = b.wave[in >= 0 ? in : 0];
   const float4* __restrict__ sh = b.sh[shIn >= 0 ? shIn : 0];
   const uint32_t lane = threadIdx.x & 31;
-  Walk w;
-  uint32_t stack[32];
+  typename WalkOf<kWide>::type w;
+  typename WalkOf<kWide>::Entry stack[WalkOf<kWide>::kDepth];
   bool has = false, drained = false, any = false;
   uint32_t item = 0, nnE = 0, ntE = 0, nnS = 0, ntS = 0;
   for (;;) {
@@ -621,17 +624,17 @@ __global__ void __launch_bounds__(kBlock) k_shade(DevScene S, FrameArgs a, Rende
 // applied before the next bounce is shaded), so results are identical.
 enum : uint32_t { kIdle = 0, kPathExt = 1, kPathShadow = 2 };
 
-template <bool kCount, int kMinBlocks>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_tail(DevScene S, FrameArgs a, RenderBuffers b, int in, int shIn,
-                                                 uint32_t depth0, uint32_t kRefill) {
+template <bool kCount, bool kWide>
+__global__ void __launch_bounds__(kBlock, 2) k_tail(DevScene S, FrameArgs a, RenderBuffers b, int in, int shIn,
+                                                   uint32_t depth0, uint32_t kRefill) {
   const uint32_t n = b.ctr->wave[in];
   const uint32_t cacheSize = b.ctr->cacheSize[a.cacheSel];
   const float4* __restrict__ cache = b.cache[a.cacheSel];
   const float4* __restrict__ sh = b.sh[shIn >= 0 ? shIn : 0];
   const Wave wv = b.wave[in];
   const uint32_t lane = threadIdx.x & 31;
-  Walk w;
-  uint32_t stack[32];
+  typename WalkOf<kWide>::type w;
+  typename WalkOf<kWide>::Entry stack[WalkOf<kWide>::kDepth];
   PathIO io;
   uint32_t mode = kIdle, depth = 0;
   bool drained = false;
@@ -832,8 +835,23 @@ __global__ void k_trace_rays(DevScene S, const float* rays, uint32_t n, float ma
   const float* r = rays + 6 * (size_t)i;
   TraceHit h;
   uint32_t nn = 0, nt = 0;
-  bool hit = trace_ref<false, kCount>(S, mk(r[0], r[1], r[2]), mk(r[3], r[4], r[5]), maxDist, eps, cullback != 0,
-                                      h, nn, nt);
+  bool hit;
+  if (S.traversal == 1 && S.wide && !cullback) {  // wide order (no back-face culling there)
+    Walk4 wk;
+    uint2 stack[kWideDepth];
+    wk.init(mk(r[0], r[1], r[2]), mk(r[3], r[4], r[5]), maxDist, eps, stack);
+    while (!wk.step<kCount>(S, stack, false, nn, nt)) {
+    }
+    hit = wk.hit();
+    h.t = wk.minT;
+    h.tri = wk.best;
+    h.w = wk.bw;
+    h.u = wk.bu;
+    h.v = wk.bv;
+  } else {
+    hit = trace_ref<false, kCount>(S, mk(r[0], r[1], r[2]), mk(r[3], r[4], r[5]), maxDist, eps, cullback != 0, h,
+                                   nn, nt);
+  }
   t[i] = hit ? h.t : -1.f;
   tri[i] = hit ? (int32_t)h.tri : -1;
   w[i] = hit ? h.w : 0.f;
@@ -897,54 +915,30 @@ cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream
   return cudaGetLastError();
 }
 
-// Resident CTAs per SM the walk kernels are compiled for (register caps
-// 64 / 48 / 40 for k_walk, 128 / 80 for k_tail); GBPT_WALK_MINB /
-// GBPT_TAIL_MINB select a variant (tuning knobs).  Measured on the 1024x768
-// interior (depth 10) and the 1280x720 hall (depth 5): k_walk at 5 CTAs per
-// SM (48 registers) is 1-2% faster than 4 and 6; k_tail at 2 and 3 tie.
-int walk_minb() {
-  static int v = [] {
-    const char* e = std::getenv("GBPT_WALK_MINB");
-    int x = e ? std::atoi(e) : 5;
-    return x >= 6 ? 6 : x == 5 ? 5 : 4;
-  }();
-  return v;
-}
-int tail_minb() {
-  static int v = [] {
-    const char* e = std::getenv("GBPT_TAIL_MINB");
-    int x = e ? std::atoi(e) : 2;
-    return x >= 3 ? 3 : 2;
-  }();
-  return v;
-}
-
-template <bool kCount, int kMinB>
+template <bool kCount, bool kWide>
 void walk_variant(const DevScene& S, const RenderBuffers& b, int in, int shIn, int shReset, uint32_t sd,
                   cudaStream_t st) {
-  static uint32_t g = grid_for((const void*)k_walk<kCount, kMinB>);
-  k_walk<kCount, kMinB><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, sd, walk_refill());
+  static uint32_t g = grid_for((const void*)k_walk<kCount, kWide>);
+  k_walk<kCount, kWide><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, sd, walk_refill());
 }
 
-template <bool kCount, int kMinB>
+template <bool kCount, bool kWide>
 void tail_variant(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn, uint32_t depth0,
                   cudaStream_t st) {
-  static uint32_t g = grid_for((const void*)k_tail<kCount, kMinB>);
-  k_tail<kCount, kMinB><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill());
+  static uint32_t g = grid_for((const void*)k_tail<kCount, kWide>);
+  k_tail<kCount, kWide><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill());
 }
 
 cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
                         int shReset, bool shDirect, cudaStream_t st) {
   const uint32_t sd = (a.bilat && shDirect) ? 1u : 0u;
-  const int mb = walk_minb();
+  const bool wide = S.traversal == 1 && S.wide;
   if (a.counting) {
-    if (mb == 6) walk_variant<true, 6>(S, b, in, shIn, shReset, sd, st);
-    else if (mb == 5) walk_variant<true, 5>(S, b, in, shIn, shReset, sd, st);
-    else walk_variant<true, 4>(S, b, in, shIn, shReset, sd, st);
+    if (wide) walk_variant<true, true>(S, b, in, shIn, shReset, sd, st);
+    else walk_variant<true, false>(S, b, in, shIn, shReset, sd, st);
   } else {
-    if (mb == 6) walk_variant<false, 6>(S, b, in, shIn, shReset, sd, st);
-    else if (mb == 5) walk_variant<false, 5>(S, b, in, shIn, shReset, sd, st);
-    else walk_variant<false, 4>(S, b, in, shIn, shReset, sd, st);
+    if (wide) walk_variant<false, true>(S, b, in, shIn, shReset, sd, st);
+    else walk_variant<false, false>(S, b, in, shIn, shReset, sd, st);
   }
   note_launches(1);
   return cudaGetLastError();
@@ -952,13 +946,13 @@ cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffe
 
 cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
                         uint32_t depth0, cudaStream_t st) {
-  const int mb = tail_minb();
+  const bool wide = S.traversal == 1 && S.wide;
   if (a.counting) {
-    if (mb == 3) tail_variant<true, 3>(S, a, b, in, shIn, depth0, st);
-    else tail_variant<true, 2>(S, a, b, in, shIn, depth0, st);
+    if (wide) tail_variant<true, true>(S, a, b, in, shIn, depth0, st);
+    else tail_variant<true, false>(S, a, b, in, shIn, depth0, st);
   } else {
-    if (mb == 3) tail_variant<false, 3>(S, a, b, in, shIn, depth0, st);
-    else tail_variant<false, 2>(S, a, b, in, shIn, depth0, st);
+    if (wide) tail_variant<false, true>(S, a, b, in, shIn, depth0, st);
+    else tail_variant<false, false>(S, a, b, in, shIn, depth0, st);
   }
   note_launches(1);
   return cudaGetLastError();

@@ -15,13 +15,24 @@ namespace gbpt {
 // so a hit reads one contiguous record instead of RTTriangle + 3 RTVertex.
 // Materials: {diffuse.xyz, transparency} {emissive.xyz, specular}
 //            {metallic, roughness, 0, 0}.
+//
+// Wide traversal (opt-in, gbpt_scene_set_traversal): the same tree collapsed
+// to 4 children per node (each node's children are its binary grandchildren,
+// or its binary children where those are leaves); 8 float4 per node:
+//   {lo.x[4]} {lo.y[4]} {lo.z[4]} {hi.x[4]} {hi.y[4]} {hi.z[4]} {code[4]} {0}
+// code: kWideEmpty, kWideTri | first triangle (a one-triangle leaf),
+// kWideLeaf | binary node id (other leaves), or a wide node index.
+constexpr uint32_t kWideEmpty = 0xFFFFFFFFu, kWideLeaf = 0x80000000u, kWideTri = 0xC0000000u;
 struct DevScene {
   const float4* nodes = nullptr;
   const float4* tris = nullptr;
   const float4* shade = nullptr;
   const float4* mats = nullptr;
   const uint32_t* lightTri = nullptr;
+  const float4* wide = nullptr;  // collapsed 4-wide tree (wide traversal only)
   uint32_t nodeN = 0, triN = 0, lightN = 0, matN = 0;
+  uint32_t wideN = 0;
+  uint32_t traversal = 0;        // 0: the reference's order (default), 1: wide
 };
 
 // Counters shared by the kernels of one renderer (device memory).

@@ -218,4 +218,161 @@ struct Walk {
   __device__ __forceinline__ bool hit() const { return minT < maxDist; }
 };
 
+// Wide walk (DevScene::traversal == 1): the collapsed 4-ary tree, one wide
+// node per step -- one 112-byte fetch and four box tests (the reference's
+// IntersectAABB arithmetic) -- children accepted when their entry distance
+// is at most the closest hit so far, pushed far to near so the nearest is
+// walked next.  The closest hit is the reference's: a triangle is accepted
+// when strictly closer, or equally close with a larger index (the
+// reference's right-first order reaches larger indices first and keeps the
+// first of equal distances; inside one leaf it walks triangles in index
+// order, so there the smaller index wins).  Stack entries are {code, entry
+// distance}.
+constexpr uint32_t kWideDepth = 56;      // >= 3 * (binary depth cap 32) / 2 + 1
+constexpr uint32_t kWideStepCap = 8192;  // pops; a wide pop replaces up to three binary ones
+struct Walk4 {
+  gb::f3 o, d, inv, oe;
+  float minT, maxDist, eps;
+  float bw, bu, bv;
+  uint32_t best, bestLeaf, steps;  // bestLeaf: first triangle of the leaf holding best
+  uint2 tos;
+  int sp;
+
+  __device__ __forceinline__ void init(gb::f3 o_, gb::f3 d_, float maxDist_, float eps_, uint2* stack) {
+    using namespace gb;
+    (void)stack;
+    o = o_;
+    d = d_;
+    inv = mk(rcp_(escape_zero(d.x)), rcp_(escape_zero(d.y)), rcp_(escape_zero(d.z)));
+    eps = eps_;
+    oe = o + eps * d;
+    maxDist = maxDist_;
+    minT = maxDist_;
+    best = 0;
+    bestLeaf = 0;
+    bw = bu = bv = 0.f;
+    steps = 0;
+    sp = 0;
+    tos = make_uint2(0u, 0u);  // wide root, entry distance 0
+  }
+
+  __device__ __forceinline__ float box(float lx, float ly, float lz, float hx, float hy, float hz) const {
+    using namespace gb;
+    const float t0x = (lx - o.x) * inv.x, t1x = (hx - o.x) * inv.x;
+    const float t0y = (ly - o.y) * inv.y, t1y = (hy - o.y) * inv.y;
+    const float t0z = (lz - o.z) * inv.z, t1z = (hz - o.z) * inv.z;
+    const float minmax = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+    const float maxmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
+    float tb = kInf;
+    if (minmax >= maxmin && (minmax > 0.f || maxmin > 0.f)) tb = (maxmin > kGtEps9) ? maxmin : 0.f;
+    return tb;
+  }
+
+  template <bool kCount>
+  __device__ __forceinline__ bool step(const DevScene& S, uint2* stack, bool anyHit, uint32_t& nNodes,
+                                       uint32_t& nTris) {
+    using namespace gb;
+    if (sp < 0 || steps >= kWideStepCap) return true;
+    steps++;
+    const uint2 e = tos;
+    sp--;
+    if (sp >= 0) tos = stack[sp];
+    if (!(__uint_as_float(e.y) <= minT)) return sp < 0;
+    const uint32_t code = e.x;
+    if (code & kWideLeaf) {
+      uint32_t first, cnt;
+      if (code & 0x40000000u) {
+        first = code & 0x3FFFFFFFu;
+        cnt = 1;
+      } else {
+        const uint32_t nid = code & 0x7FFFFFFFu;
+        first = __float_as_uint(__ldg(S.nodes + 2 * (size_t)nid).w);
+        cnt = __float_as_uint(__ldg(S.nodes + 2 * (size_t)nid + 1).w);
+      }
+      for (uint32_t i = first; i < first + cnt; i++) {
+        float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), e0 = p0, e1 = p0;
+        if (i < S.triN) {
+          p0 = __ldg(S.tris + 3 * (size_t)i);
+          e0 = __ldg(S.tris + 3 * (size_t)i + 1);
+          e1 = __ldg(S.tris + 3 * (size_t)i + 2);
+        }
+        if (kCount) nTris++;
+        const f3 E0 = mk(e0.x, e0.y, e0.z), E1 = mk(e1.x, e1.y, e1.z);
+        const f3 de2 = cross(d, E1);
+        float div = dot(de2, E0);
+        if (fabsf(div) < kLtEps9) continue;
+        div = rcp_(div);
+        const f3 t = oe - mk(p0.x, p0.y, p0.z);
+        const f3 te1 = cross(t, E0);
+        const float rT = dot(te1, E1) * div;
+        if (rT < 0.f) continue;
+        const float u = dot(de2, t) * div;
+        if (u < 0.f || u > 1.f) continue;
+        const float v = dot(te1, d) * div;
+        if (v < 0.f || (u + v) > 1.f) continue;
+        if (rT < minT || (rT == minT && minT < maxDist && first > bestLeaf)) {
+          minT = rT;
+          best = i;
+          bestLeaf = first;
+          bw = 1.f - u - v;
+          bu = u;
+          bv = v;
+          if (anyHit) return true;
+        }
+      }
+      return sp < 0;
+    }
+    if (kCount) nNodes++;
+    const float4* r = S.wide + 8 * (size_t)code;
+    const float4 lx = __ldg(r), ly = __ldg(r + 1), lz = __ldg(r + 2);
+    const float4 hx = __ldg(r + 3), hy = __ldg(r + 4), hz = __ldg(r + 5);
+    const uint4 cd = __ldg(reinterpret_cast<const uint4*>(r + 6));
+    float t[4] = {box(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x), box(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y),
+                  box(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z), box(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w)};
+    uint32_t c[4] = {cd.x, cd.y, cd.z, cd.w};
+    uint32_t m = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const bool ok = c[k] != kWideEmpty && t[k] < kInf && t[k] <= minT;
+      if (!ok) t[k] = __uint_as_float(0x7f800000u);  // +inf sorts last
+      m += ok ? 1u : 0u;
+    }
+    // sort the four (distance, code) pairs, nearest first
+#define GB_CSWAP(a, b)                   \
+  if (t[b] < t[a]) {                     \
+    const float tt = t[a];               \
+    t[a] = t[b];                         \
+    t[b] = tt;                           \
+    const uint32_t cc = c[a];            \
+    c[a] = c[b];                         \
+    c[b] = cc;                           \
+  }
+    GB_CSWAP(0, 1) GB_CSWAP(2, 3) GB_CSWAP(0, 2) GB_CSWAP(1, 3) GB_CSWAP(1, 2)
+#undef GB_CSWAP
+    if (m == 0) return sp < 0;
+    if (sp + (int)m >= (int)kWideDepth) m = (uint32_t)((int)kWideDepth - 1 - sp);  // keep the nearest
+    // far to near below the new top; the nearest becomes the top (stack[sp] keeps the old top)
+    for (uint32_t j = m - 1; j >= 1; j--) stack[sp + (int)(m - j)] = make_uint2(c[j], __float_as_uint(t[j]));
+    sp += (int)m;
+    tos = make_uint2(c[0], __float_as_uint(t[0]));
+    return false;
+  }
+
+  __device__ __forceinline__ bool hit() const { return minT < maxDist; }
+};
+
+// walk type, stack entry type and stack depth of the two traversal orders
+template <bool kWide>
+struct WalkOf {
+  using type = Walk;
+  using Entry = uint32_t;
+  static constexpr int kDepth = 32;
+};
+template <>
+struct WalkOf<true> {
+  using type = Walk4;
+  using Entry = uint2;
+  static constexpr int kDepth = (int)kWideDepth;
+};
+
 }  // namespace gbpt

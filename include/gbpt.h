@@ -151,6 +151,15 @@ gbpt_status gbpt_scene_destroy(gbpt_scene* s);
 gbpt_status gbpt_scene_build_bvh(gbpt_scene* s, uint32_t max_depth, uint32_t threads, double* build_seconds);
 /* updateAllSceneMaterialsCudaMem (src/cudaRTCommon.cu:580-599) and the
  * light-triangle rescan updateLightTriCudaMem (src/cudaRTBDPTStream.cu:57-77). */
+/* BVH walk order.  0 (default): the reference's TracePrimitive order
+ * (src/cudaRTCommon.cu:66-127): hits, node and triangle counts bit-exact.
+ * 1: wide -- the same tree collapsed to 4 children per node, nearest child
+ * first, boxes culled against the closest hit so far; the closest hit is the
+ * same triangle (ties go to the one the reference reaches first, the larger
+ * triangle index) except where the reference's limits cut its walk short
+ * (2048 pops, 29-deep stack) or surfaces lie closer together than the 1e-4
+ * origin push; node counts differ.  Restarts progressive accumulation. */
+gbpt_status gbpt_scene_set_traversal(gbpt_scene* s, int32_t traversal);
 gbpt_status gbpt_scene_update_materials(gbpt_scene* s, const gbpt_material* mats, uint32_t nm);
 /* CompactBVH export (include/bvhhelper.h:45-54): node count first (pass NULL
  * arrays), then bounds[6*nodeN] (min xyz, max xyz), offOrTSTN[2*nodeN],

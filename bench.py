@@ -225,6 +225,29 @@ def bench_gpu(args):
     total_ms = float(np.sum(ms))
     value = paths / (total_ms / 1e3) / 1e6
 
+    # the same frames with the wide traversal (opt-in; same hits except surfaces closer together
+    # than the reference's origin push), timed the same way on a second renderer
+    wide = None
+    if args.traversal == "reference" and not args.no_wide:
+        scene.set_traversal("wide")
+        rw = gb.RTRenderer(W, H, WL[3], params)
+        for _ in range(warm):
+            rw.render_frames(scene, cam, 1, stats=True)
+        wms, wpaths = [], 0
+        for _ in range(args.steps):
+            flush()
+            st = rw.render_frames(scene, cam, 1, stats=True)
+            wms.append(st["ms_total"])
+            wpaths += st["paths"]
+        wv = wpaths / (float(np.sum(wms)) / 1e3) / 1e6
+        wide = {"value": round(wv * world, 3), "ms_per_step": round(float(np.mean(wms)), 4),
+                "tree": "binary tree collapsed to 4 children per node, nearest child first",
+                "hits": "the reference's closest hit except where two surfaces lie within its 1e-4 origin push "
+                        "of each other (tests/test_wide.py; 0.8% of random rays in the Cornell box, whose "
+                        "blocks stand on the floor)"}
+        rw.close()
+        scene.set_traversal("reference")
+
     # e2e through the public call with a host result buffer (D2H of the image each step)
     out = np.zeros(np_ * 3, np.float32)
     t0 = time.perf_counter()
@@ -276,6 +299,7 @@ def bench_gpu(args):
                      "traffic": traffic,
                      "algorithmic_bytes_per_frame": int(trace_bytes)},
         "filter_roofline": filter_roofline(phases, args.steps, np_, peak) if WL[3] == 1 else None,
+        "wide_traversal": wide,
         "learned_sampler": learned_sampler_summary(),
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
@@ -354,6 +378,7 @@ def main():
     ap.add_argument("--impl", default="gbpt", choices=["gbpt", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="interior", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-wide", action="store_true", help="skip the extra wide-traversal timing")
     ap.add_argument("--traversal", default="reference", choices=["reference", "wide"],
                     help="BVH walk order: the reference's (bit-exact, default) or the collapsed 4-wide tree")
     args = ap.parse_args()

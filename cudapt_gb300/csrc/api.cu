@@ -575,7 +575,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   // launches would each wait for their slowest ray)
   int in = 0;
   const uint32_t D = a.eyeDepth;
-  const uint32_t K = std::min(tail_from(D), D);
+  const uint32_t K = std::min(tail_from(D, S.traversal == 1 && S.wide), D);
   for (uint32_t d = 0; d < K; d++) {
     CK(launch_walk(S, a, r->rb, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), d == 1, st));
     mark(r, kPhTrace, timing);

@@ -958,16 +958,18 @@ cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffe
   return cudaGetLastError();
 }
 
-uint32_t tail_from(uint32_t eyeDepth) {
-  // default: the last 4 bounces (measured on the 1024x768 interior, depth 10:
-  // tail kernel from bounce 6 beats both per-bounce launches throughout and
-  // earlier switches; the tail kernel's 107 registers cost occupancy while
-  // many paths are alive)
+uint32_t tail_from(uint32_t eyeDepth, bool wide) {
+  // default, reference order: the last 4 bounces (measured on the 1024x768
+  // interior, depth 10: the tail kernel from bounce 6 beats both per-bounce
+  // launches throughout and earlier switches; its ~120 registers cost
+  // occupancy while many paths are alive).  Wide order: no tail (its walks
+  // are short enough that per-bounce launches win: 150.8 against 141.7
+  // Mpaths/s from bounce 6 and 124.0 from bounce 5).
   static int v = [] {
     const char* e = std::getenv("GBPT_TAIL_FROM");
     return e ? std::atoi(e) : -2;
   }();
-  if (v == -2) return eyeDepth > 6 ? eyeDepth - 4 : eyeDepth;
+  if (v == -2) return (!wide && eyeDepth > 6) ? eyeDepth - 4 : eyeDepth;
   return v < 0 ? eyeDepth : (uint32_t)v;
 }
 

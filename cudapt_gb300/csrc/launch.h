@@ -112,8 +112,9 @@ cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuff
 // with the connection attached to it in queue shIn; one lane per path
 cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
                         uint32_t depth0, cudaStream_t st);
-// first bounce handled by the tail kernel (GBPT_TAIL_FROM, < 0: never; default D-4 for D > 6)
-uint32_t tail_from(uint32_t eyeDepth);
+// first bounce handled by the tail kernel (GBPT_TAIL_FROM, < 0: never; default D-4 for D > 6
+// in the reference order, never in the wide order)
+uint32_t tail_from(uint32_t eyeDepth, bool wide);
 cudaError_t launch_apply(const FrameArgs& a, const RenderBuffers& b, float* result, uint32_t* sampleN, float* gpos,
                          float* gnorm, float* gdiff, cudaStream_t st);
 // filter-only mode (src/cudaRTBDPTStreamBilat.cu:989-1051): running means of

@@ -161,6 +161,11 @@ __device__ __forceinline__ void st_bf16(uint8_t* base, uint32_t off, float x) {
   *reinterpret_cast<__nv_bfloat16*>(base + off) = __float2bfloat16_rn(x);
 }
 
+__device__ __forceinline__ float warp_sum(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 __device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
 __device__ __forceinline__ float gelu_grad(float z) {
   return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * expf(-0.5f * z * z) * 0.39894228040143268f;
@@ -236,7 +241,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_forward(const float* __rest
     mma_issue(tmem + tD1, smem_u32(sm + sAx), 32, smem_u32(sm + sBw1), 32, 64, 2);
     mma_commit(bar);
   }
-  ok = mbar_wait(bar, phase);
+  ok = __syncthreads_and(mbar_wait(bar, phase) ? 1 : 0) != 0;  // block-uniform
   if (ok) phase ^= 1u;
   tc_after();
   const uint32_t lane0 = (warp * 32u) << 16;
@@ -256,7 +261,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_forward(const float* __rest
     mma_commit(bar);
   }
   if (ok) {
-    ok = mbar_wait(bar, phase);
+    ok = __syncthreads_and(mbar_wait(bar, phase) ? 1 : 0) != 0;  // block-uniform
     if (ok) phase ^= 1u;
     tc_after();
   }
@@ -331,7 +336,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_train(const float* __restri
     mma_issue(tmem + tD1, smem_u32(sm + sAx), 32, smem_u32(sm + sBw1), 32, 64, 2);
     mma_commit(bar);
   }
-  ok = mbar_wait(bar, phase);
+  ok = __syncthreads_and(mbar_wait(bar, phase) ? 1 : 0) != 0;  // block-uniform
   if (ok) phase ^= 1u;
   tc_after();
   if (ok) {
@@ -355,7 +360,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_train(const float* __restri
     mma_commit(bar);
   }
   if (ok) {
-    ok = mbar_wait(bar, phase);
+    ok = __syncthreads_and(mbar_wait(bar, phase) ? 1 : 0) != 0;  // block-uniform
     if (ok) phase ^= 1u;
     tc_after();
   }
@@ -368,12 +373,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_train(const float* __restri
       yv += gelu(z2[j]) * vec[128 + j];
     }
     const float dy = valid ? 2.f * (yv - target) / (float)n : 0.f;
-    if (valid) atomicAdd(&sscal[1], (yv - target) * (yv - target));
-    atomicAdd(&sscal[0], dy);
+    // column sums over the CTA's rows: a warp butterfly, then one shared atomic per warp
+    const float l2 = warp_sum(valid ? (yv - target) * (yv - target) : 0.f), sdy = warp_sum(dy);
+    if ((t & 31) == 0) {
+      atomicAdd(&sscal[1], l2);
+      atomicAdd(&sscal[0], sdy);
+    }
     for (int j = 0; j < 64; j++) {
-      atomicAdd(&sdw3[j], dy * gelu(z2[j]));
+      const float g3 = warp_sum(dy * gelu(z2[j]));
       const float dz = dy * vec[128 + j] * gelu_grad(z2[j]);
-      atomicAdd(&sdb2[j], dz);
+      const float g2 = warp_sum(dz);
+      if ((t & 31) == 0) {
+        atomicAdd(&sdw3[j], g3);
+        atomicAdd(&sdb2[j], g2);
+      }
       st_bf16(sm + sAdz2, kmaj(t, j, 64), dz);
       st_bf16(sm + sAdz2t, kmaj(j, t, 128), dz);
     }
@@ -389,7 +402,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_train(const float* __restri
     mma_commit(bar);
   }
   if (ok) {
-    ok = mbar_wait(bar, phase);
+    ok = __syncthreads_and(mbar_wait(bar, phase) ? 1 : 0) != 0;  // block-uniform
     if (ok) phase ^= 1u;
     tc_after();
   }
@@ -400,7 +413,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_train(const float* __restri
       tmem_ld16(tmem + lane0 + tD1 + c, z1);
       for (int j = 0; j < 16; j++) {
         const float dz = dh[j] * gelu_grad(z1[j] + vec[c + j]);
-        atomicAdd(&sdb1[c + j], dz);
+        const float g1 = warp_sum(dz);
+        if ((t & 31) == 0) atomicAdd(&sdb1[c + j], g1);
         st_bf16(sm + sAdz1t, kmaj(c + j, t, 128), dz);
       }
     }
@@ -422,7 +436,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_train(const float* __restri
     mma_commit(bar);
   }
   if (ok) {
-    ok = mbar_wait(bar, phase);
+    ok = __syncthreads_and(mbar_wait(bar, phase) ? 1 : 0) != 0;  // block-uniform
     if (ok) phase ^= 1u;
     tc_after();
   }

@@ -255,6 +255,7 @@ struct gbpt_renderer {
     dfree(ab.partial);
     dfree(ab.filtered);
     dfree(ab.coop);
+    dfree(ab.heavy);
     dfree(result);
     dfree(gpos);
     dfree(gnorm);
@@ -360,6 +361,7 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   CK(dalloc(&r->ab.partial, adapt_reduce_blocks((uint32_t)np)));
   CK(dalloc(&r->ab.filtered, np * 3));
   CK(dalloc(&r->ab.coop, kCoopWords));
+  CK(dalloc(&r->ab.heavy, np));
   CK(cudaMemsetAsync(r->ab.coop, 0, kCoopWords * 4, r->st));
   for (float* b : {r->result, r->gpos, r->gnorm, r->gdiff, r->ab.filtered, r->gemis, r->direct, r->filtered2,
                    r->probView})

@@ -294,29 +294,24 @@ __global__ void k_gen_adapt(FrameArgs a, RenderBuffers b, const uint32_t* __rest
   }
 }
 
-// Per-pixel sums of the budgeted samples, then the running means.  One warp
-// per pixel: lane l adds samples l, l+32, l+64, ... in slot order, then the
-// 32 partial sums are combined by a butterfly (x += shfl_xor(x, m) for
-// m = 16, 8, 4, 2, 1).  The order is a fixed function of the sample count, so
-// the result does not depend on timing, and a pixel with thousands of
-// samples costs one warp pass instead of a serial loop.
-__device__ __forceinline__ float bfly(float v) {
-  for (int m = 16; m > 0; m >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, m);
-  return v;
-}
+// Per-pixel sums of the budgeted samples, then the running means.  The sum
+// order is a fixed function of the pixel's sample count c, so results do not
+// depend on timing (the reference adds with float atomics in arbitrary
+// order): P(c) partial sums -- partial l adds samples l, l+P, l+2P, ... in
+// slot order -- combined by a butterfly (x[l] += x[l ^ m] for m = P/2 .. 1),
+// with P = 8 for c <= 64, 32 for c <= 4096 and 1024 above.  The budget
+// spreads one frame's W*H samples very unevenly (a firefly pixel can take
+// tens of thousands), so each range has its own kernel: eight lanes per pixel
+// (four pixels per warp) for the many light pixels, a warp per pixel for the
+// medium ones, a 1024-thread CTA per pixel for the heaviest; the last two
+// take their pixels from lists the first kernel appends to.
+constexpr uint32_t kAccumSmall = 64, kAccumMid = 4096;
+constexpr uint32_t kHugeThreads = 1024;
 
 template <bool kMoments>
-__global__ void k_accum(FrameArgs a, RenderBuffers b, const uint32_t* __restrict__ off,
-                        const uint32_t* __restrict__ cnt, float* result, uint32_t* sampleN, float* gpos,
-                        float* gnorm, float* gdiff) {
-  const uint32_t np = a.width * a.height;
-  const uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t lane = threadIdx.x & 31;
-  if (p >= np) return;  // warp-uniform
-  float v[15] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  uint32_t tN = 0;
-  const uint32_t o = off[p], c = cnt[p];
-  for (uint32_t s = o + lane; s < o + c; s += 32) {
+__device__ __forceinline__ void accum_partials(const RenderBuffers& b, uint32_t o, uint32_t c, uint32_t l, uint32_t P,
+                                               float* v, uint32_t& tN) {
+  for (uint32_t s = o + l; s < o + c; s += P) {
     float4 r = b.res[s];
     if (isinf(r.x) || isinf(r.y) || isinf(r.z)) continue;
     uint32_t n = __float_as_uint(r.w);
@@ -331,9 +326,13 @@ __global__ void k_accum(FrameArgs a, RenderBuffers b, const uint32_t* __restrict
     }
     tN += n;
   }
-  for (int k = 0; k < (kMoments ? 15 : 12); k++) v[k] = bfly(v[k]);
-  for (int m = 16; m > 0; m >>= 1) tN += __shfl_xor_sync(0xffffffffu, tN, m);
-  if (lane != 0) return;
+}
+
+// running means of pixel p from its summed samples (one thread)
+template <bool kMoments>
+__device__ __forceinline__ void accum_write(const FrameArgs& a, const RenderBuffers& b, uint32_t p, const float* v,
+                                            uint32_t tN, float* result, uint32_t* sampleN, float* gpos,
+                                            float* gnorm, float* gdiff) {
   float* q = result + 3 * (size_t)p;
   float* P = gpos + 3 * (size_t)p;
   float* Nn = gnorm + 3 * (size_t)p;
@@ -359,6 +358,90 @@ __global__ void k_accum(FrameArgs a, RenderBuffers b, const uint32_t* __restrict
     N = nn;
   }
   sampleN[p] = N;
+}
+
+// light pixels, eight lanes each; heavier pixels are listed for the next kernels
+template <bool kMoments>
+__global__ void k_accum(FrameArgs a, RenderBuffers b, AdaptBuffers ab, float* result, uint32_t* sampleN, float* gpos,
+                        float* gnorm, float* gdiff) {
+  const uint32_t np = a.width * a.height;
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t p = gid >> 3, l = gid & 7u;
+  if ((gid & ~31u) >= np * 8u) return;  // whole warps past the image only
+  uint32_t c = p < np ? ab.cnt[p] : 0u;
+  if (c > kAccumSmall) {
+    if (l == 0) {
+      if (c <= kAccumMid)
+        ab.heavy[atomicAdd(&b.ctr->heavyMid, 1u)] = p;
+      else
+        ab.heavy[np - 1u - atomicAdd(&b.ctr->heavyHuge, 1u)] = p;
+    }
+    c = 0;
+  }
+  float v[15] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  uint32_t tN = 0;
+  if (c) accum_partials<kMoments>(b, ab.off[p], c, l, 8, v, tN);
+  for (int k = 0; k < (kMoments ? 15 : 12); k++)
+    for (int m = 4; m > 0; m >>= 1) v[k] = v[k] + __shfl_xor_sync(0xffffffffu, v[k], m);
+  for (int m = 4; m > 0; m >>= 1) tN += __shfl_xor_sync(0xffffffffu, tN, m);
+  if (l == 0 && p < np && ab.cnt[p] <= kAccumSmall) accum_write<kMoments>(a, b, p, v, tN, result, sampleN, gpos, gnorm, gdiff);
+}
+
+// medium pixels: a warp each, 32 partials
+template <bool kMoments>
+__global__ void k_accum_mid(FrameArgs a, RenderBuffers b, AdaptBuffers ab, float* result, uint32_t* sampleN,
+                            float* gpos, float* gnorm, float* gdiff) {
+  const uint32_t nMid = b.ctr->heavyMid;
+  const uint32_t lane = threadIdx.x & 31u;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nMid; w += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t p = ab.heavy[w];
+    float v[15] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    uint32_t tN = 0;
+    accum_partials<kMoments>(b, ab.off[p], ab.cnt[p], lane, 32, v, tN);
+    for (int k = 0; k < (kMoments ? 15 : 12); k++)
+      for (int m = 16; m > 0; m >>= 1) v[k] = v[k] + __shfl_xor_sync(0xffffffffu, v[k], m);
+    for (int m = 16; m > 0; m >>= 1) tN += __shfl_xor_sync(0xffffffffu, tN, m);
+    if (lane == 0) accum_write<kMoments>(a, b, p, v, tN, result, sampleN, gpos, gnorm, gdiff);
+  }
+}
+
+// the heaviest pixels: a 1024-thread CTA each, 1024 partials; butterfly steps
+// m >= 32 exchange through shared memory, the rest through shuffles
+template <bool kMoments>
+__global__ void __launch_bounds__(kHugeThreads) k_accum_huge(FrameArgs a, RenderBuffers b, AdaptBuffers ab,
+                                                             float* result, uint32_t* sampleN, float* gpos,
+                                                             float* gnorm, float* gdiff) {
+  __shared__ float xs[kHugeThreads];
+  __shared__ uint32_t ns[kHugeThreads];
+  const uint32_t np = a.width * a.height;
+  const uint32_t nHuge = b.ctr->heavyHuge;
+  const uint32_t t = threadIdx.x;
+  for (uint32_t h = blockIdx.x; h < nHuge; h += gridDim.x) {
+    const uint32_t p = ab.heavy[np - 1u - h];
+    float v[15] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    uint32_t tN = 0;
+    accum_partials<kMoments>(b, ab.off[p], ab.cnt[p], t, kHugeThreads, v, tN);
+    for (int k = 0; k < (kMoments ? 15 : 12); k++) {
+      float x = v[k];
+      for (uint32_t m = kHugeThreads / 2; m >= 32; m >>= 1) {
+        xs[t] = x;
+        __syncthreads();
+        const float y = xs[t ^ m];
+        __syncthreads();
+        x = x + y;
+      }
+      for (int m = 16; m > 0; m >>= 1) x = x + __shfl_xor_sync(0xffffffffu, x, m);
+      v[k] = x;
+    }
+    ns[t] = tN;
+    __syncthreads();
+    if (t == 0) {
+      uint32_t total = 0;
+      for (uint32_t i = 0; i < kHugeThreads; i++) total += ns[i];
+      accum_write<kMoments>(a, b, p, v, total, result, sampleN, gpos, gnorm, gdiff);
+    }
+    __syncthreads();
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -780,12 +863,20 @@ cudaError_t launch_mlp_alloc(const FrameArgs& a, const AdaptBuffers& ab, cudaStr
 cudaError_t launch_adapt_accum(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab, float* result,
                                uint32_t* sampleN, float* gpos, float* gnorm, float* gdiff, cudaStream_t st) {
   const uint32_t np = a.width * a.height;
-  const uint32_t g = (uint32_t)(((size_t)np * 32 + 255) / 256);
-  if (a.moments)
-    k_accum<true><<<g, 256, 0, st>>>(a, b, ab.off, ab.cnt, result, sampleN, gpos, gnorm, gdiff);
-  else
-    k_accum<false><<<g, 256, 0, st>>>(a, b, ab.off, ab.cnt, result, sampleN, gpos, gnorm, gdiff);
-  note_launches(1);
+  const uint32_t g = (uint32_t)(((size_t)np * 8 + 255) / 256);
+  cudaError_t e = cudaMemsetAsync(&b.ctr->heavyMid, 0, 2 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  const uint32_t gm = (uint32_t)sm_count() * 8, gh = (uint32_t)sm_count();
+  if (a.moments) {
+    k_accum<true><<<g, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
+    k_accum_mid<true><<<gm, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
+    k_accum_huge<true><<<gh, kHugeThreads, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
+  } else {
+    k_accum<false><<<g, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
+    k_accum_mid<false><<<gm, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
+    k_accum_huge<false><<<gh, kHugeThreads, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
+  }
+  note_launches(3);
   return cudaGetLastError();
 }
 

@@ -43,7 +43,8 @@ struct DevCounters {
   uint32_t paths;         // camera paths of the current frame
   uint32_t errFlags;      // bit 0: light cache overflow, bit 1: bounds
   uint32_t fetchT;        // next ray handed to a lane by the persistent walk kernel
-  uint32_t fetchS;        // unused (kept for layout)
+  uint32_t heavyMid;      // adaptive accumulation: pixels listed for the warp-per-pixel pass
+  uint32_t heavyHuge;     // ... and for the CTA-per-pixel pass
   unsigned long long rays, nodes, tris;  // cumulative work counters (closest-hit walks)
   unsigned long long shadowRays, nodesS, trisS;  // any-hit (shadow) walks
   double errSum;          // adaptive: sum of per-pixel errors
@@ -145,6 +146,7 @@ struct AdaptBuffers {
   float* feat;         // learned allocator: 24 features per 8x8 tile
   float* pred;         // learned allocator: log budget weight per tile
   float* tileErr;      // learned allocator: sum of the heuristic error over each tile
+  uint32_t* heavy;     // W*H: pixels with many budgeted samples (medium ones from the front, heaviest from the back)
 };
 constexpr uint32_t kFeatures = 24;
 constexpr uint32_t kErrMlpTimeout = 256u;  // DevCounters::errFlags bit: an MLP tensor-core wait ran out

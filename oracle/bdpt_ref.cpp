@@ -1132,21 +1132,22 @@ void render_frame(Renderer* r, const Scene& s, const Camera& cam) {
   }
   // per-pixel sums (pt_atomicApplyPathQueueResult_kernel :1041-1085, then
   // pt_accumTempResultToResult_kernel :1088-1141) in the library's fixed
-  // order: 32 lane partials (lane l adds samples l, l+32, ...), then a
-  // butterfly x[l] = x[l] + x[l^m] for m = 16, 8, 4, 2, 1.
+  // order: P partials (partial l adds samples l, l+P, ...; P = 8 for up to 64
+  // samples, 32 for up to 4096, 1024 above), then a butterfly
+  // x[l] = x[l] + x[l^m] for m = P/2, ..., 1.
   size_t q = 0;
+  std::vector<float> part, nxt;
+  std::vector<uint32_t> pn, nn2;
   for (uint32_t i = 0; i < np; i++) {
-    float part[32][12];
-    uint32_t pn[32];
-    for (int l = 0; l < 32; l++) {
-      pn[l] = 0;
-      for (int k = 0; k < 12; k++) part[l][k] = 0.f;
-    }
-    for (uint32_t k = 0; k < r->counts[i]; k++) {
+    const uint32_t cnt = r->counts[i];
+    const uint32_t P = cnt <= 64 ? 8u : cnt <= 4096 ? 32u : 1024u;
+    part.assign((size_t)P * 12, 0.f);
+    pn.assign(P, 0u);
+    for (uint32_t k = 0; k < cnt; k++) {
       const PathResult& pr = res[q + k];
       float a[3] = {(float)pr.acc[0], (float)pr.acc[1], (float)pr.acc[2]};
       if (std::isinf(a[0]) || std::isinf(a[1]) || std::isinf(a[2])) continue;
-      float* v = part[k & 31];
+      float* v = &part[(size_t)(k % P) * 12];
       float fn = (float)pr.n;
       for (int c3 = 0; c3 < 3; c3++) {
         v[c3] = v[c3] + a[c3];
@@ -1154,27 +1155,25 @@ void render_frame(Renderer* r, const Scene& s, const Camera& cam) {
         v[6 + c3] = v[6 + c3] + (float)pr.gnorm[c3] * fn;
         v[9 + c3] = v[9 + c3] + (float)pr.gdiff[c3] * fn;
       }
-      pn[k & 31] += pr.n;
+      pn[k % P] += pr.n;
     }
-    q += r->counts[i];
-    for (int m = 16; m > 0; m >>= 1) {
-      float nxt[32][12];
-      uint32_t nn2[32];
-      for (int l = 0; l < 32; l++) {
-        for (int k = 0; k < 12; k++) nxt[l][k] = part[l][k] + part[l ^ m][k];
+    q += cnt;
+    for (uint32_t m = P / 2; m > 0; m >>= 1) {
+      nxt.assign((size_t)P * 12, 0.f);
+      nn2.assign(P, 0u);
+      for (uint32_t l = 0; l < P; l++) {
+        for (int k = 0; k < 12; k++) nxt[(size_t)l * 12 + k] = part[(size_t)l * 12 + k] + part[(size_t)(l ^ m) * 12 + k];
         nn2[l] = pn[l] + pn[l ^ m];
       }
-      for (int l = 0; l < 32; l++) {
-        pn[l] = nn2[l];
-        for (int k = 0; k < 12; k++) part[l][k] = nxt[l][k];
-      }
+      part.swap(nxt);
+      pn.swap(nn2);
     }
     float tr[3], tp[3], tn[3], td[3];
     for (int c3 = 0; c3 < 3; c3++) {
-      tr[c3] = part[0][c3];
-      tp[c3] = part[0][3 + c3];
-      tn[c3] = part[0][6 + c3];
-      td[c3] = part[0][9 + c3];
+      tr[c3] = part[c3];
+      tp[c3] = part[3 + c3];
+      tn[c3] = part[6 + c3];
+      td[c3] = part[9 + c3];
     }
     uint32_t tN = pn[0];
     uint32_t N = r->sampleN[i];

@@ -142,6 +142,25 @@ def test_adaptive_matches(gbdev, orc):
     assert abs(img.mean() - want.mean()) <= 2e-3 * want.mean()
 
 
+def test_adaptive_accumulation_tiers(gbdev, orc):
+    """The per-pixel sums of budgeted frames use 8, 32 or 1024 partials by
+    sample count (kernels k_accum / k_accum_mid / k_accum_huge); the oracle
+    sums in the same order, so frames stay bit-identical across the tiers."""
+    r, ref, img, want, stats = _render_both(gbdev, orc, "cornell", 192, 160, 4, mode=1, eye_depth_max=8,
+                                            light_depth_max=8, warmup_frames=2, filter_radius=4)
+    cnt = ref.sample_counts()[1]
+    assert cnt.max() > 64  # the warp-per-pixel tier ran
+    same = np.mean(img.view(np.uint32) == want.view(np.uint32))
+    assert same >= 0.99, same
+    np.testing.assert_array_equal(r.read_buffer(6), ref.sample_counts()[0])
+    # the hall's fireflies draw most of a frame's budget onto single pixels: the CTA-per-pixel tier
+    r, ref, img, want, stats = _render_both(gbdev, orc, "hall_small", 256, 144, 8, mode=1, eye_depth_max=5,
+                                            light_depth_max=5, warmup_frames=5, filter_radius=4)
+    assert ref.sample_counts()[1].max() > 4096, ref.sample_counts()[1].max()
+    same = np.mean(img.view(np.uint32) == want.view(np.uint32))
+    assert same >= 0.99, same
+
+
 def test_adaptive_binary_matches(gbdev, orc):
     """'BDPTSC Adap Bilat Binary': window search passes, leftover fill, per-pass apply."""
     r, ref, img, want, stats = _render_both(gbdev, orc, "cornell", 64, 48, 5, mode=2, eye_depth_max=8,

@@ -12,14 +12,23 @@
 //     `<` against the closest hit (first triangle wins ties).
 // The per-ray constants of those two tests (1/escapeZero(dir), o + eps*dir)
 // are hoisted out of the loop; they are the same values every iteration.
-// Node and triangle fetches are read-only 16-byte __ldg loads (one 32-byte
-// sector per node); an out-of-range id reads zeros like the reference's
-// texture fetch.
+// A node is fetched with one 32-byte non-coherent load (ld.global.nc.v8, one
+// sector; sm_100 and later), a triangle with three 16-byte __ldg loads; an
+// out-of-range id reads zeros like the reference's texture fetch.
 #pragma once
 #include "gbpt_math.cuh"
 #include "launch.h"
 
 namespace gbpt {
+
+// Both halves of a 32-byte node record (min.xyz + word, max.xyz + word).
+// `p` is 32-byte aligned: node arrays start on cudaMalloc's 256-byte
+// boundary and a record is 32 bytes.
+__device__ __forceinline__ void ldg_node(const float4* p, float4& a, float4& b) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
 
 struct TraceHit {
   float t, w, u, v;
@@ -45,8 +54,7 @@ __device__ __forceinline__ bool trace_ref(const DevScene& S, gb::f3 o, gb::f3 d,
     const uint32_t cur = stack[sp--];
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
     if (cur < S.nodeN) {
-      a = __ldg(nodes + 2 * (size_t)cur);
-      b = __ldg(nodes + 2 * (size_t)cur + 1);
+      ldg_node(nodes + 2 * (size_t)cur, a, b);
     }
     if (kCount) nNodes++;
     const float t0x = (a.x - o.x) * inv.x, t1x = (b.x - o.x) * inv.x;
@@ -159,8 +167,7 @@ struct Walk {
     if (sp >= 0) tos = stack[sp];
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
     if (cur < S.nodeN) {
-      a = __ldg(S.nodes + 2 * (size_t)cur);
-      b = __ldg(S.nodes + 2 * (size_t)cur + 1);
+      ldg_node(S.nodes + 2 * (size_t)cur, a, b);
     }
     if (kCount) nNodes++;
     const float t0x = (a.x - o.x) * inv.x, t1x = (b.x - o.x) * inv.x;
@@ -324,8 +331,10 @@ struct Walk4 {
     }
     if (kCount) nNodes++;
     const float4* r = S.wide + 8 * (size_t)code;
-    const float4 lx = __ldg(r), ly = __ldg(r + 1), lz = __ldg(r + 2);
-    const float4 hx = __ldg(r + 3), hy = __ldg(r + 4), hz = __ldg(r + 5);
+    float4 lx, ly, lz, hx, hy, hz;
+    ldg_node(r, lx, ly);
+    ldg_node(r + 2, lz, hx);
+    ldg_node(r + 4, hy, hz);
     const uint4 cd = __ldg(reinterpret_cast<const uint4*>(r + 6));
     float t[4] = {box(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x), box(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y),
                   box(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z), box(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w)};

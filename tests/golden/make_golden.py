@@ -10,6 +10,7 @@ Outputs (all produced by the CPU oracle, FP32 float contract):
   obj_cornell.npz   mesh, BVH (bounds/offsets/order) and 1024 traced rays
   cornell_frames.npz 3 progressive frames of a 24x24 plain-BDPT render and
                      the light-vertex cache of frame 0
+  empty_children.npz a 38-triangle scene whose tree has empty children
   obj_cornell_glass.npz the OBJ with its MTL materials, the sphere made glass
                      as the reference's cornellwtranball preset does, and that
                      preset's camera (a scene with refraction and total
@@ -71,6 +72,27 @@ def main(ref_root):
     cam3 = pre["camera"]
     np.savez_compressed(os.path.join(HERE, "obj_cornell_glass.npz"), vertices=v3, triangles=t3, materials=m3,
                         cam=oracle.cam_array(cam3))
+    # a small scene whose binned-SAH tree has empty children (kept as (start, 0)
+    # records that the reference's walk treats as inner nodes): the first
+    # scene of a seeded search of clustered triangles where the oracle's
+    # builder reports empty children
+    rng = np.random.Generator(np.random.PCG64(0))
+    for _ in range(5000):
+        n = int(rng.integers(3, 40))
+        cen = rng.normal(size=(n, 3)) * rng.choice([1e-3, 1.0, 100.0], size=(n, 1))
+        if rng.random() < 0.5:
+            cen[: n // 2] = cen[0]
+        tri = cen[:, None, :] + rng.normal(size=(n, 3, 3)) * rng.choice([1e-4, 0.5, 20], size=(n, 1, 1))
+        v4 = np.zeros(n * 3, layouts.VERTEX)
+        v4["pos"] = tri.reshape(-1, 3).astype(np.float32)
+        t4 = np.zeros(n, layouts.TRIANGLE)
+        t4["v0"] = np.arange(n) * 3
+        t4["v1"] = t4["v0"] + 1
+        t4["v2"] = t4["v0"] + 2
+        m4 = np.zeros(1, layouts.MATERIAL)
+        if oracle.Scene(v4, t4, m4).empty_children > 0:
+            np.savez_compressed(os.path.join(HERE, "empty_children.npz"), vertices=v4, triangles=t4, materials=m4)
+            break
     print("wrote", os.listdir(HERE))
 
 

@@ -96,3 +96,17 @@ def test_compact_layout_invariants(gb):
     for i in idx[:2000]:
         for c in (i + 1, i + o[i, 0]):
             assert np.all(b[c, :3] >= b[i, :3]) and np.all(b[c, 3:] <= b[i, 3:])
+
+
+def _empty_children_scene():
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "empty_children.npz"))
+    return g["vertices"], g["triangles"], g["materials"]
+
+
+def test_bvh_empty_children_fixture(gb, orc):
+    """A tree with empty children ((start, 0) records the reference's walk
+    enters as inner nodes, src/bvhhelper.cpp): built identically."""
+    v, t, m = _empty_children_scene()
+    s, ref = _compare(gb, orc, v, t, m)
+    assert ref.empty_children > 0

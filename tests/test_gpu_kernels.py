@@ -1,5 +1,6 @@
 """GPU parity of the building blocks: device math, Philox, BVH traversal."""
 import math
+import os
 
 import numpy as np
 import pytest
@@ -72,6 +73,22 @@ def test_trace_bitexact_camera(gbdev, orc, name):
     rays = camera_rays(cam, 320, 240, seed=12)
     got, ref = _trace_both(gbdev, orc, v, t, m, rays)
     _assert_same_hits(got, ref)
+
+
+def test_trace_bitexact_empty_children(gbdev, orc):
+    """A tree with empty children keeps the reference's node order on the
+    device (the right-first relayout needs every inner node to have two real
+    subtrees); hits and visit counts still equal the oracle's."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "empty_children.npz"))
+    v, t, m = g["vertices"], g["triangles"], g["materials"]
+    assert orc.Scene(v, t, m).empty_children > 0
+    rays = random_rays(v, 100_000, seed=15, pad=1.0)
+    got, ref = _trace_both(gbdev, orc, v, t, m, rays)
+    assert (ref["tri"] >= 0).mean() > 0.01
+    _assert_same_hits(got, ref)
+    for kw in (dict(eps=1e-4), dict(cullback=True)):
+        got, ref = _trace_both(gbdev, orc, v, t, m, rays, **kw)
+        _assert_same_hits(got, ref)
 
 
 def test_trace_variants(gbdev, orc):

@@ -115,6 +115,25 @@ class RTScene:
         return out
 
 
+_PAGE = 4096
+
+
+def _host_floats(n):
+    """A zeroed float32 host array of n values on whole pages of its own,
+    page-locked through gbpt_host_register when CUDA allows it (the result
+    copy of gbpt_render then runs at link speed).  Returns (array, the
+    registered address or None)."""
+    nbytes = n * 4
+    span = -(-nbytes // _PAGE) * _PAGE
+    raw = np.zeros(span + _PAGE, np.uint8)
+    off = (-raw.ctypes.data) % _PAGE
+    arr = raw[off:off + nbytes].view(np.float32)
+    addr = raw.ctypes.data + off
+    if load().gbpt_host_register(ctypes.c_void_p(addr), span) != 0:
+        return arr, None
+    return arr, ctypes.c_void_p(addr)
+
+
 class RTRenderer:
     """``RTRenderer`` (include/raytracer.h:292-323) for the BDPT modes.
 
@@ -131,7 +150,7 @@ class RTRenderer:
         check(L.gbpt_renderer_create(self.width, self.height, int(mode), ptr(p), ctypes.addressof(h)))
         self._h = h
         self._mode = int(mode)
-        self._out = np.zeros(self.width * self.height * 3, np.float32)
+        self._out, self._pinned = _host_floats(self.width * self.height * 3)
         self.last_stats = None
 
     # reference-style names
@@ -194,6 +213,9 @@ class RTRenderer:
         if getattr(self, "_h", None) and self._h.value:
             load().gbpt_renderer_destroy(self._h)
             self._h = ctypes.c_void_p()
+        if getattr(self, "_pinned", None):
+            load().gbpt_host_unregister(self._pinned)  # the array stays valid, as pageable memory
+            self._pinned = None
 
     def __del__(self):
         try:

@@ -80,6 +80,8 @@ SIGNATURES = {
     "gbpt_render_frames": (i32, [vp, vp, vp, u32, vp]),
     "gbpt_result": (ctypes.POINTER(ctypes.c_float), [vp]),
     "gbpt_read_buffer": (i32, [vp, i32, vp, ctypes.c_size_t, i32]),
+    "gbpt_host_register": (i32, [vp, ctypes.c_size_t]),
+    "gbpt_host_unregister": (i32, [vp]),
     "gbpt_reset": (i32, [vp]),
     "gbpt_clean": (i32, [vp]),
     "gbpt_set_counting": (i32, [vp, i32]),

@@ -211,7 +211,8 @@ struct gbpt_renderer {
   const float* bilatOut = nullptr;  // filter plane holding the last filtered image
   uint32_t* sampleN = nullptr;
   float4* waveMem = nullptr;
-  std::vector<float> hostResult;
+  float* hostResult = nullptr;  // page-locked copy of the current view (gbpt_result)
+  size_t hostResultN = 0;
   uint32_t frame = 0;
   bool started = false;
   float camBasis[9] = {0};
@@ -273,6 +274,9 @@ struct gbpt_renderer {
     bilatOut = nullptr;
     dfree(gauss);
     dfree(sampleN);
+    if (hostResult) cudaFreeHost(hostResult);
+    hostResult = nullptr;
+    hostResultN = 0;
     alloc = false;
   }
   ~gbpt_renderer() {
@@ -370,7 +374,9 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   r->bilatOut = r->ab.filtered;
   CK(cudaMemsetAsync(r->sampleN, 0, np * 4, r->st));
   CK(cudaMemsetAsync(r->ab.err, 0, np * 4, r->st));
-  r->hostResult.assign(np * 3, 0.f);
+  CK(cudaMallocHost((void**)&r->hostResult, np * 12));
+  std::memset(r->hostResult, 0, np * 12);
+  r->hostResultN = np * 3;
   r->alloc = true;
   r->gaussKey[0] = r->gaussKey[1] = -1.f;
   return GBPT_OK;
@@ -1007,8 +1013,7 @@ gbpt_status gbpt_renderer_destroy(gbpt_renderer* r) {
 
 gbpt_status gbpt_set_mode(gbpt_renderer* r, int32_t mode) {
   if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
-  if (mode < GBPT_MODE_BDPT_SC || mode > GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY)
-    return fail(GBPT_ERR_INVALID_ARG, "unknown renderer mode");
+  if (mode < GBPT_MODE_BDPT_SC || mode > GBPT_MODE_PT_SC) return fail(GBPT_ERR_INVALID_ARG, "unknown renderer mode");
   if (mode != r->mode) {
     r->mode = mode;
     r->started = false;  // RTRenderer::SetRendererMode starts the new renderer from scratch
@@ -1038,10 +1043,7 @@ gbpt_status gbpt_get_params(const gbpt_renderer* r, gbpt_params* params) {
 
 gbpt_status gbpt_render(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, float* out_rgb,
                         int32_t out_is_device, gbpt_stats* stats) {
-  gbpt_status st = render_impl(r, s, cam, 1, out_rgb, out_is_device, stats);
-  if (st != GBPT_OK || out_rgb == nullptr || out_is_device) return st;
-  std::memcpy(r->hostResult.data(), out_rgb, r->hostResult.size() * 4);
-  return GBPT_OK;
+  return render_impl(r, s, cam, 1, out_rgb, out_is_device, stats);
 }
 
 gbpt_status gbpt_render_frames(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, uint32_t frames,
@@ -1053,9 +1055,21 @@ const float* gbpt_result(gbpt_renderer* r) {
   if (!r || !r->alloc) return nullptr;
   // the image gbpt_render copies out (the mode's current view), as the reference's GetResult returns
   if (cudaStreamSynchronize(r->st) != cudaSuccess ||
-      cudaMemcpy(r->hostResult.data(), output_view(r), r->hostResult.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+      cudaMemcpy(r->hostResult, output_view(r), r->hostResultN * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
     return nullptr;
-  return r->hostResult.data();
+  return r->hostResult;
+}
+
+gbpt_status gbpt_host_register(void* p, size_t bytes) {
+  if (!p || bytes == 0) return fail(GBPT_ERR_INVALID_ARG, "NULL or empty host range");
+  CK(cudaHostRegister(p, bytes, cudaHostRegisterDefault));
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_host_unregister(void* p) {
+  if (!p) return fail(GBPT_ERR_INVALID_ARG, "NULL host pointer");
+  CK(cudaHostUnregister(p));
+  return GBPT_OK;
 }
 
 gbpt_status gbpt_read_buffer(gbpt_renderer* r, int32_t which, void* dst, size_t bytes, int32_t dst_is_device) {

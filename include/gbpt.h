@@ -195,9 +195,16 @@ gbpt_status gbpt_render(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam,
 /* Adds `frames` passes without copying (benchmarks / progressive runs). */
 gbpt_status gbpt_render_frames(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, uint32_t frames,
                                gbpt_stats* stats);
-/* RTRenderer::GetResult (include/raytracer.h:311): library-owned host copy of
- * the last result (refreshed by gbpt_render / gbpt_read_result). */
+/* RTRenderer::GetResult (include/raytracer.h:311): library-owned, page-locked
+ * host copy of the current result view, read from the device on each call
+ * (NULL before the first pass or on a CUDA error). */
 const float* gbpt_result(gbpt_renderer* r);
+/* Page-lock (cudaHostRegister) / release a caller-owned host range, so that
+ * gbpt_render's out_rgb copy into it runs at link speed rather than through a
+ * staging buffer.  Optional: unregistered host memory works, more slowly.
+ * Ranges must not overlap a registered page of another range. */
+gbpt_status gbpt_host_register(void* p, size_t bytes);
+gbpt_status gbpt_host_unregister(void* p);
 /* Copies a renderer buffer: 0 result RGB, 1 first-hit position, 2 normal,
  * 3 diffuse (G-buffer: count-weighted means in the adaptive modes, the last
  * frame's first hit in BDPT_SC_BILAT), 4 filtered RGB, 5 per-pixel error

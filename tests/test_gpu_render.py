@@ -235,3 +235,25 @@ def test_fp32_converges_to_fp64_reference(gbdev, orc):
         assert rmse_same < 0.15 * rmse_indep, (F, rmse_same, rmse_indep)
         ref64[F, "indep"] = rmse_indep
     assert ref64[32, "indep"] < ref64[8, "indep"]
+
+
+def test_mode_switch_and_result_buffers(gbdev):
+    """SetRendererMode reaches every registered renderer; the image gbpt_render
+    copies into the caller's page-locked buffer equals GetResult's copy."""
+    (v, t, m), cam = scene_arrays("cornell")
+    s = gbdev.RTScene(v, t, m).build_bvh()
+    r = gbdev.RTRenderer(32, 32, 0, gbdev.default_params(eye_depth_max=4, light_depth_max=4))
+    assert r._pinned is not None
+    L = gbdev._native.load()
+    for mode in (0, 3, 4, 1, 2):
+        r.SetRendererMode(mode)
+        img = r.render(s, cam)
+        got = np.ctypeslib.as_array(L.gbpt_result(r.handle), shape=(32 * 32 * 3,))
+        assert np.array_equal(img.view(np.uint32), got.view(np.uint32)), mode
+        assert np.isfinite(img).all() and img.max() > 0
+    with pytest.raises(gbdev.GbptError) as e:
+        r.SetRendererMode(5)
+    assert e.value.status == 1
+    r.close()
+    assert r._pinned is None
+    img[:] = 0  # still valid memory after the release

@@ -277,6 +277,10 @@ def bench_gpu(args):
                "sample": f"{W}x{rows} rows (4 bands spread over the frame) of one uniform frame, oracle FP32 estimator "
                          f"({bs:.2f} s restated BVH build)"}
 
+    serving = None
+    if rank == 0 and not args.no_serving:
+        serving = serving_run(gb)
+
     D = int(params["eye_depth_max"])
     traffic = profiled_traffic(args.workload)
     line = {
@@ -301,12 +305,36 @@ def bench_gpu(args):
         "filter_roofline": filter_roofline(phases, args.steps, np_, peak) if WL[3] == 1 else None,
         "wide_traversal": wide,
         "learned_sampler": learned_sampler_summary(),
+        "serving": serving,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": launches,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def serving_run(gb, n=64, rate=200.0, seed=0, workers=4):
+    """The batched-serving configuration: n requests arriving as a Poisson
+    process (rate per second), each a scene of the three plain benchmark
+    scenes, a resolution of {128^2, 256^2, 512^2, 1024x768}, {4, 16, 64}
+    spp and depth cap {6, 8, 10}; BVHs resident on the device, `workers`
+    requests in flight (cudapt_gb300.serving)."""
+    from cudapt_gb300 import scenes, serving
+    objs, cams = {}, {}
+    for name in ("cornell", "interior", "hall"):
+        (v, t, m), cam = getattr(scenes, name)()
+        objs[name] = gb.RTScene(v, t, m).build_bvh()
+        cams[name] = cam
+    wl = serving.poisson_workload(n, rate, seed)
+    summary, st = serving.run_poisson(gb, wl, objs, cams, workers=workers)
+    summary["config"] = (f"{n} requests, Poisson {rate:g}/s (seed {seed}), scenes cornell/interior/hall, "
+                         "resolution in {128^2, 256^2, 512^2, 1024x768}, spp in {4, 16, 64}, depth in {6, 8, 10}, "
+                         "plain BDPT, image copied to page-locked host memory per request")
+    summary["unit"] = "Mpaths/s (all requests' camera paths / wall time from first arrival to last completion)"
+    for s_ in objs.values():
+        s_.close()
+    return summary
 
 
 def filter_roofline(phases, steps, np_, peak):
@@ -379,6 +407,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="interior", choices=sorted(WORKLOADS))
     ap.add_argument("--no-wide", action="store_true", help="skip the extra wide-traversal timing")
+    ap.add_argument("--no-serving", action="store_true", help="skip the batched-serving run")
     ap.add_argument("--traversal", default="reference", choices=["reference", "wide"],
                     help="BVH walk order: the reference's (bit-exact, default) or the collapsed 4-wide tree")
     args = ap.parse_args()

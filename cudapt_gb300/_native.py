@@ -57,6 +57,41 @@ class Stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Request(ctypes.Structure):
+    """gbpt_request (80 bytes)."""
+    _fields_ = [
+        ("scene", ctypes.c_void_p),
+        ("camera", ctypes.c_float * 10),
+        ("width", ctypes.c_uint32),
+        ("height", ctypes.c_uint32),
+        ("frames", ctypes.c_uint32),
+        ("mode", ctypes.c_int32),
+        ("params", ctypes.c_void_p),
+        ("out_rgb", ctypes.c_void_p),
+    ]
+
+
+class RequestStatus(ctypes.Structure):
+    """gbpt_request_status (56 bytes)."""
+    _fields_ = [
+        ("id", ctypes.c_uint64),
+        ("status", ctypes.c_int32),
+        ("done", ctypes.c_uint32),
+        ("queued_ms", ctypes.c_double),
+        ("run_ms", ctypes.c_double),
+        ("latency_ms", ctypes.c_double),
+        ("paths", ctypes.c_uint64),
+        ("walk_refill", ctypes.c_uint32),
+        ("tail_from", ctypes.c_int32),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+assert ctypes.sizeof(Request) == 80 and ctypes.sizeof(RequestStatus) == 56
+
+
 # every exported entry point of include/gbpt.h with its ctypes signature
 vp, u32, i32, f32, f64p = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int32, ctypes.c_float, ctypes.c_void_p
 SIGNATURES = {
@@ -82,6 +117,11 @@ SIGNATURES = {
     "gbpt_read_buffer": (i32, [vp, i32, vp, ctypes.c_size_t, i32]),
     "gbpt_host_register": (i32, [vp, ctypes.c_size_t]),
     "gbpt_host_unregister": (i32, [vp]),
+    "gbpt_server_create": (i32, [u32, ctypes.c_uint64, vp]),
+    "gbpt_server_destroy": (i32, [vp]),
+    "gbpt_server_submit": (i32, [vp, vp, vp]),
+    "gbpt_server_wait": (i32, [vp, ctypes.c_uint64, u32, vp]),
+    "gbpt_server_tuned": (i32, [vp, i32, u32, u32, u32, vp, vp, vp]),
     "gbpt_reset": (i32, [vp]),
     "gbpt_clean": (i32, [vp]),
     "gbpt_set_counting": (i32, [vp, i32]),

@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgbpt.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels_wave.cu", "kernels_adapt.cu", "api.cu", "noalloc.cu", "image.cu", "mlp.cu", "bvh_build.cpp"]
+SOURCES = ["kernels_wave.cu", "kernels_adapt.cu", "api.cu", "noalloc.cu", "image.cu", "mlp.cu", "bvh_build.cpp",
+           "server.cpp"]
 
 
 def _nvcc():
@@ -64,7 +65,7 @@ def build(force=False, verbose=False):
             if verbose and err:
                 print(err)
     if jobs or not os.path.exists(LIB):
-        link = [_nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-lcudart"]
+        link = [_nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-lcudart", "-lpthread"]
         r = subprocess.run(link, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + " ".join(link) + "\n" + r.stdout + r.stderr)

@@ -76,6 +76,7 @@ struct gbpt_scene {
   DevScene dev;
   uint64_t version = 0;
   bool uploaded = false;
+  std::mutex upload;  // renderers on several threads (a server's workers) may upload it first
 
   void free_dev() {
     dfree(dNodes);
@@ -181,6 +182,7 @@ gbpt_status upload_scene(gbpt_scene* s) {
 
 gbpt_status ensure_uploaded(gbpt_scene* s) {
   if (!s->built) return fail(GBPT_ERR_STATE, "scene has no BVH (call gbpt_scene_build_bvh)");
+  std::lock_guard<std::mutex> lock(s->upload);
   if (s->uploaded) return GBPT_OK;
   return upload_scene(s);
 }
@@ -303,8 +305,20 @@ gbpt_status check_params(const gbpt_params* p) {
   if (p->filter_radius > 31) return fail(GBPT_ERR_INVALID_ARG, "filter_radius must be <= 31");
   if (p->bilat_radius > 31) return fail(GBPT_ERR_INVALID_ARG, "bilat_radius must be <= 31");
   if (p->pt_depth_max < 1 || p->pt_depth_max > 64) return fail(GBPT_ERR_INVALID_ARG, "pt_depth_max must be 1..64");
+  if (p->walk_refill > 32) return fail(GBPT_ERR_INVALID_ARG, "walk_refill must be 0..32");
+  if (p->tail_from < -1) return fail(GBPT_ERR_INVALID_ARG, "tail_from must be >= -1");
   return GBPT_OK;
 }
+
+}  // namespace
+
+uint64_t gbpt::renderer_bytes(uint32_t W, uint32_t H, const gbpt_params& p) {
+  const size_t np = (size_t)W * H;
+  const uint32_t cacheCap = std::max(1u, p.light_paths * (1 + p.light_depth_max));
+  return np * (128 + 16 + 96 + 16 + 48 + 16 + 8) + np * (12 * 10 + 4 * 2 + 4 * 4) + (size_t)cacheCap * 192;
+}
+
+namespace {
 
 gbpt_status ensure_alloc(gbpt_renderer* r) {
   if (r->alloc) return GBPT_OK;
@@ -312,7 +326,7 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   const size_t cap = np;
   const uint32_t cacheCap = std::max(1u, r->p.light_paths * (1 + r->p.light_depth_max));
   // admission: refuse when the buffers cannot fit in free HBM
-  size_t need = cap * (128 + 16 + 96 + 16 + 48 + 16 + 8) + np * (12 * 10 + 4 * 2 + 4 * 4) + (size_t)cacheCap * 192;
+  const size_t need = renderer_bytes(r->W, r->H, r->p);
   size_t freeB = 0, totB = 0;
   CK(cudaMemGetInfo(&freeB, &totB));
   if (need + (64ull << 20) > freeB)
@@ -503,6 +517,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   const bool learned = r->mlp != nullptr && r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT;
   a.moments = (learned || (r->collect && adaptive)) ? 1u : 0u;
   a.tilesX = (r->W + 7) / 8;
+  a.refill = r->p.walk_refill;
   if (a.moments && r->frame == 0)
     CK(cudaMemsetAsync(r->rb.hist, 0, (size_t)a.tilesX * ((r->H + 7) / 8) * 32, r->st));
   a.counting = r->counting ? 1u : 0u;
@@ -583,7 +598,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   // launches would each wait for their slowest ray)
   int in = 0;
   const uint32_t D = a.eyeDepth;
-  const uint32_t K = std::min(tail_from(D, S.traversal == 1 && S.wide), D);
+  const uint32_t K = std::min(tail_from(D, S.traversal == 1 && S.wide, r->p.tail_from), D);
   for (uint32_t d = 0; d < K; d++) {
     CK(launch_walk(S, a, r->rb, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), d == 1, st));
     mark(r, kPhTrace, timing);
@@ -665,9 +680,11 @@ gbpt_status render_impl(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam,
   CK(cudaGetLastError());
   {  // device-side error words (bounded waits, bounds checks): report once, then clear
     uint32_t flags = 0;
-    CK(cudaMemcpy(&flags, &r->rb.ctr->errFlags, 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(&flags, &r->rb.ctr->errFlags, 4, cudaMemcpyDeviceToHost, r->st));
+    CK(cudaStreamSynchronize(r->st));
     if (flags) {
-      CK(cudaMemset(&r->rb.ctr->errFlags, 0, 4));
+      CK(cudaMemsetAsync(&r->rb.ctr->errFlags, 0, 4, r->st));
+      CK(cudaStreamSynchronize(r->st));
       if (flags & 4u) return fail(GBPT_ERR_TIMEOUT, "grid barrier of the binary allocator timed out");
       if (flags & kErrMlpTimeout) return fail(GBPT_ERR_TIMEOUT, "learned allocator: tensor-core wait timed out");
       return fail(GBPT_ERR_BOUNDS, "device bounds check tripped (light cache)");
@@ -822,6 +839,8 @@ gbpt_status gbpt_params_default(gbpt_params* p) {
   p->filter_iterations = 1;
   p->render_iterations = 5;
   p->pt_depth_max = 10;
+  p->walk_refill = 0;
+  p->tail_from = -1;
   return GBPT_OK;
 }
 

@@ -34,6 +34,9 @@ gbpt_status rmse_device(const float* a, const float* b, uint64_t n, double* out,
 gbpt_status mlp_forward_async(gbpt_mlp* m, const float* x, uint32_t n, float* y, uint32_t* err, uint32_t errBit,
                               void* stream);
 
+// device bytes a renderer of this size allocates (its admission figure)
+uint64_t renderer_bytes(uint32_t W, uint32_t H, const gbpt_params& p);
+
 // thread-local error text (gbpt_last_error_string)
 void set_error(const std::string& s);
 gbpt_status fail(gbpt_status st, const std::string& s);

@@ -917,28 +917,29 @@ cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream
 
 template <bool kCount, bool kWide>
 void walk_variant(const DevScene& S, const RenderBuffers& b, int in, int shIn, int shReset, uint32_t sd,
-                  cudaStream_t st) {
+                  uint32_t refill, cudaStream_t st) {
   static uint32_t g = grid_for((const void*)k_walk<kCount, kWide>);
-  k_walk<kCount, kWide><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, sd, walk_refill());
+  k_walk<kCount, kWide><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, sd, refill);
 }
 
 template <bool kCount, bool kWide>
 void tail_variant(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn, uint32_t depth0,
                   cudaStream_t st) {
   static uint32_t g = grid_for((const void*)k_tail<kCount, kWide>);
-  k_tail<kCount, kWide><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill());
+  k_tail<kCount, kWide><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill_for(a.refill));
 }
 
 cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
                         int shReset, bool shDirect, cudaStream_t st) {
   const uint32_t sd = (a.bilat && shDirect) ? 1u : 0u;
   const bool wide = S.traversal == 1 && S.wide;
+  const uint32_t rf = walk_refill_for(a.refill);
   if (a.counting) {
-    if (wide) walk_variant<true, true>(S, b, in, shIn, shReset, sd, st);
-    else walk_variant<true, false>(S, b, in, shIn, shReset, sd, st);
+    if (wide) walk_variant<true, true>(S, b, in, shIn, shReset, sd, rf, st);
+    else walk_variant<true, false>(S, b, in, shIn, shReset, sd, rf, st);
   } else {
-    if (wide) walk_variant<false, true>(S, b, in, shIn, shReset, sd, st);
-    else walk_variant<false, false>(S, b, in, shIn, shReset, sd, st);
+    if (wide) walk_variant<false, true>(S, b, in, shIn, shReset, sd, rf, st);
+    else walk_variant<false, false>(S, b, in, shIn, shReset, sd, rf, st);
   }
   note_launches(1);
   return cudaGetLastError();
@@ -958,7 +959,7 @@ cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffe
   return cudaGetLastError();
 }
 
-uint32_t tail_from(uint32_t eyeDepth, bool wide) {
+uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested) {
   // default, reference order: the last 4 bounces (measured on the 1024x768
   // interior, depth 10: the tail kernel from bounce 6 beats both per-bounce
   // launches throughout and earlier switches; its ~120 registers cost
@@ -969,8 +970,13 @@ uint32_t tail_from(uint32_t eyeDepth, bool wide) {
     const char* e = std::getenv("GBPT_TAIL_FROM");
     return e ? std::atoi(e) : -2;
   }();
+  if (requested >= 0) return (uint32_t)requested;
   if (v == -2) return (!wide && eyeDepth > 6) ? eyeDepth - 4 : eyeDepth;
   return v < 0 ? eyeDepth : (uint32_t)v;
+}
+
+uint32_t walk_refill_for(uint32_t requested) {
+  return (requested >= 1 && requested <= 32) ? requested : walk_refill();
 }
 
 cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t depth,

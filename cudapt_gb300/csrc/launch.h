@@ -74,6 +74,7 @@ struct FrameArgs {
   uint32_t ptsc;        // unidirectional mode: no connections, total internal reflection reflects
   uint32_t moments;     // learned allocator: per-pixel second moments and per-tile path-length counts
   uint32_t tilesX;      // 8x8 tiles per image row
+  uint32_t refill;      // idle lanes of a warp that trigger a refill in the persistent walks
 };
 
 struct RenderBuffers {
@@ -113,9 +114,13 @@ cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuff
 // with the connection attached to it in queue shIn; one lane per path
 cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
                         uint32_t depth0, cudaStream_t st);
-// first bounce handled by the tail kernel (GBPT_TAIL_FROM, < 0: never; default D-4 for D > 6
-// in the reference order, never in the wide order)
-uint32_t tail_from(uint32_t eyeDepth, bool wide);
+// first bounce handled by the tail kernel: `requested` when >= 0 (>= D: none),
+// else GBPT_TAIL_FROM when set, else D-4 for D > 6 in the reference order and
+// none in the wide order
+uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested);
+// refill threshold of the persistent walks: `requested` when 1..32, else
+// GBPT_WALK_REFILL when set, else 20
+uint32_t walk_refill_for(uint32_t requested);
 cudaError_t launch_apply(const FrameArgs& a, const RenderBuffers& b, float* result, uint32_t* sampleN, float* gpos,
                          float* gnorm, float* gdiff, cudaStream_t st);
 // filter-only mode (src/cudaRTBDPTStreamBilat.cu:989-1051): running means of

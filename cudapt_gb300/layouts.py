@@ -65,6 +65,8 @@ PARAMS = np.dtype(
         ("filter_iterations", "<u4"),
         ("render_iterations", "<u4"),
         ("pt_depth_max", "<u4"),
+        ("walk_refill", "<u4"),
+        ("tail_from", "<i4"),
     ]
 )
 
@@ -114,6 +116,8 @@ def default_params(**over):
     p["filter_iterations"] = 1
     p["render_iterations"] = 5
     p["pt_depth_max"] = 10
+    p["walk_refill"] = 0
+    p["tail_from"] = -1
     for k, v in over.items():
         p[k] = v
     return p

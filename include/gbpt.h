@@ -93,6 +93,10 @@ typedef struct gbpt_params {
   uint32_t filter_iterations; /* "Filter Iteration" (1): filter passes per frame, ping-pong */
   uint32_t render_iterations; /* "Render Iteration" (5): frames that trace paths; 0 = no limit */
   uint32_t pt_depth_max;    /* "PTSC" bounce cap, NORMALRAY_BOUND_MAX of src/cudaRTPTStream.cu:6 (10) */
+  /* scheduling of the wavefront (results do not depend on either) */
+  uint32_t walk_refill;     /* idle lanes of a warp that make a persistent walk fetch new rays (1..32; 0: 20) */
+  int32_t tail_from;        /* first bounce the per-path tail kernel carries (>= the depth cap: none;
+                               -1: depth - 4 when the cap exceeds 6 in the reference order, none in the wide order) */
 } gbpt_params;
 
 /* Renderer modes: the BDPT entries of the X-macro registry
@@ -322,6 +326,52 @@ gbpt_status gbpt_renderer_set_mlp(gbpt_renderer* r, gbpt_mlp* mlp, int32_t colle
  * out == NULL: only *n_tiles. */
 gbpt_status gbpt_renderer_features(gbpt_renderer* r, float* out, uint32_t capacity, int32_t out_is_device,
                                    uint32_t* n_tiles);
+
+/* ---- batched render serving ----------------------------------------------
+ * The reference renders one scene per process, synchronously
+ * (src/cudaRTBDPTStream.cu:134-169, 816-951).  A server takes render requests
+ * of uneven size from any thread and runs up to `workers` of them at once,
+ * each on its own renderer and CUDA stream, so that small requests fill the
+ * SMs together; scenes stay resident on the device.  A request is admitted
+ * when its renderer's buffers fit in free HBM minus `hbm_reserve_bytes`
+ * (otherwise it waits for running requests to free memory, and fails with
+ * GBPT_ERR_OOM only when nothing else runs).  Requests whose params leave
+ * walk_refill = 0 and tail_from = -1 get those scheduling knobs from the
+ * server's autotuner, which times whole requests per class (mode, depth cap,
+ * image size) and keeps the fastest candidate; the knobs change only speed,
+ * never the image. */
+typedef struct gbpt_server gbpt_server;
+typedef struct gbpt_request {
+  gbpt_scene* scene;         /* BVH built; shared by any number of requests */
+  gbpt_camera camera;
+  uint32_t width, height;
+  uint32_t frames;           /* progressive passes (samples per pixel in BDPT_SC) */
+  int32_t mode;              /* gbpt_mode */
+  const gbpt_params* params; /* NULL: defaults; copied at submission */
+  float* out_rgb;            /* NULL or a host buffer of width*height*3 floats, written on completion */
+} gbpt_request;
+typedef struct gbpt_request_status {
+  uint64_t id;
+  int32_t status;            /* GBPT_OK or the error the request ended with */
+  uint32_t done;             /* 1 once finished */
+  double queued_ms;          /* submission to start */
+  double run_ms;             /* start to completion (image on the host) */
+  double latency_ms;         /* submission to completion */
+  uint64_t paths;            /* camera paths traced */
+  uint32_t walk_refill;      /* the scheduling knobs it ran with */
+  int32_t tail_from;
+} gbpt_request_status;
+gbpt_status gbpt_server_create(uint32_t workers, uint64_t hbm_reserve_bytes, gbpt_server** out);
+/* Finishes the queued and running requests, then frees every renderer. */
+gbpt_status gbpt_server_destroy(gbpt_server* s);
+gbpt_status gbpt_server_submit(gbpt_server* s, const gbpt_request* req, uint64_t* id);
+/* Waits up to timeout_ms (0: poll) for request `id`; GBPT_ERR_TIMEOUT if it
+ * is still queued or running (out->done = 0).  A finished request's status
+ * stays readable until the server is destroyed. */
+gbpt_status gbpt_server_wait(gbpt_server* s, uint64_t id, uint32_t timeout_ms, gbpt_request_status* out);
+/* The autotuner's choice for a class: *samples requests timed so far. */
+gbpt_status gbpt_server_tuned(gbpt_server* s, int32_t mode, uint32_t depth, uint32_t width, uint32_t height,
+                              uint32_t* walk_refill, int32_t* tail_from, uint32_t* samples);
 
 /* ---- device math, exposed for verification -------------------------------
  * Evaluated by a kernel on host arrays x/out (copied in and out).

@@ -257,3 +257,28 @@ def test_mode_switch_and_result_buffers(gbdev):
     r.close()
     assert r._pinned is None
     img[:] = 0  # still valid memory after the release
+
+
+@pytest.mark.parametrize("name,W,H,depth", [("interior", 1024, 768, 10), ("hall", 1280, 720, 5)])
+def test_full_size_frame_bands_match_oracle(gbdev, orc, name, W, H, depth):
+    """The benchmark workloads at full size: one GPU frame against the
+    oracle's rendering of three 4-row bands of the same frame (every path's
+    random numbers follow from its global pixel id and the frame's light
+    cache, so a window of the image renders alone)."""
+    from cudapt_gb300 import scenes
+    (v, t, m), cam = getattr(scenes, name)()
+    params = gbdev.default_params(eye_depth_max=depth, light_depth_max=depth)
+    s = gbdev.RTScene(v, t, m).build_bvh()
+    r = gbdev.RTRenderer(W, H, 0, params)
+    img = r.render(s, cam).reshape(H, W, 3).copy()
+    assert r.last_stats["paths"] == W * H
+    osc = orc.Scene(v, t, m)
+    for y0 in (0, H // 2, H - 4):
+        ref = orc.Renderer(W, 4, 0, params)
+        ref.set_window(0, y0, W, H)
+        ref.render(osc, cam, 1)
+        want = ref.get(0).reshape(4, W, 3)
+        got = img[y0:y0 + 4]
+        same = np.mean(got.view(np.uint32) == want.view(np.uint32))
+        assert same >= 0.995, (y0, same)
+        assert abs(float(got.mean()) - float(want.mean())) <= 2e-3 * max(float(want.mean()), 1e-6)

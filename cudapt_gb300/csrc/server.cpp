@@ -9,6 +9,11 @@
 // queue is empty exits at once, so a concurrent request's CTAs take its
 // place).  Scenes are shared and stay resident.
 //
+// Order: first come first served, or (default) shortest first with aging --
+// the queued request with the least estimated run time minus time already
+// waited starts next, so a burst of small requests is not stuck behind a
+// large one and a large one is not passed over for long.
+//
 // Admission: a request starts when its renderer's device buffers fit in free
 // HBM minus the reserve; otherwise the worker first frees its own idle
 // renderers, then waits for running requests to finish, and fails the request
@@ -74,6 +79,10 @@ std::vector<Knobs> candidates(uint32_t depth) {
 
 constexpr uint32_t kTrials = 2;
 
+// run-time estimate of the shortest-first order: camera paths per ms of one
+// request alone (about the plain walk's rate on the benchmark scenes)
+constexpr double kPathsPerMs = 1e5;
+
 struct ClassKey {
   int32_t mode;
   uint32_t depth, size;  // size: ceil(log2(width * height))
@@ -129,6 +138,7 @@ struct gbpt_server {
   uint32_t running = 0;
   bool stop = false;
   int device = 0;
+  int32_t policy = GBPT_SERVE_SHORTEST_FIRST;
 
   ~gbpt_server() {
     {
@@ -287,8 +297,21 @@ void gbpt_server::worker_main() {
       std::unique_lock<std::mutex> lock(mu);
       cvWork.wait(lock, [&] { return stop || !queue.empty(); });
       if (queue.empty()) return;  // stopping, nothing left
-      req = queue.front();
-      queue.pop_front();
+      auto pick = queue.begin();
+      if (policy == GBPT_SERVE_SHORTEST_FIRST) {  // least (estimated run time - time waited)
+        const Clock::time_point now = Clock::now();
+        double bestKey = 1e300;
+        for (auto it = queue.begin(); it != queue.end(); ++it) {
+          const double key = (double)(*it)->q.width * (*it)->q.height * (*it)->q.frames / kPathsPerMs -
+                             ms_between((*it)->tSubmit, now);
+          if (key < bestKey) {
+            bestKey = key;
+            pick = it;
+          }
+        }
+      }
+      req = *pick;
+      queue.erase(pick);
       running++;
       if (req->tuned) req->knobs = assign(ClassKey{req->q.mode, req->depth(), req->size()});
     }
@@ -320,6 +343,15 @@ gbpt_status gbpt_server_create(uint32_t workers, uint64_t hbm_reserve_bytes, gbp
   s->device = dev;
   for (uint32_t i = 0; i < workers; i++) s->workers.emplace_back([s] { s->worker_main(); });
   *out = s;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_server_set_policy(gbpt_server* s, int32_t policy) {
+  if (!s) return fail(GBPT_ERR_INVALID_ARG, "server is NULL");
+  if (policy != GBPT_SERVE_FIFO && policy != GBPT_SERVE_SHORTEST_FIRST)
+    return fail(GBPT_ERR_INVALID_ARG, "unknown queue policy");
+  std::lock_guard<std::mutex> lock(s->mu);
+  s->policy = policy;
   return GBPT_OK;
 }
 

@@ -362,6 +362,11 @@ typedef struct gbpt_request_status {
   int32_t tail_from;
 } gbpt_request_status;
 gbpt_status gbpt_server_create(uint32_t workers, uint64_t hbm_reserve_bytes, gbpt_server** out);
+/* Queue order: GBPT_SERVE_FIFO, or GBPT_SERVE_SHORTEST_FIRST (default): the
+ * queued request with the least estimated run time (its camera paths at
+ * 1e5 paths per ms) minus the time it has waited starts next. */
+enum { GBPT_SERVE_FIFO = 0, GBPT_SERVE_SHORTEST_FIRST = 1 };
+gbpt_status gbpt_server_set_policy(gbpt_server* s, int32_t policy);
 /* Finishes the queued and running requests, then frees every renderer. */
 gbpt_status gbpt_server_destroy(gbpt_server* s);
 gbpt_status gbpt_server_submit(gbpt_server* s, const gbpt_request* req, uint64_t* id);

@@ -259,6 +259,7 @@ struct gbpt_renderer {
     dfree(ab.filtered);
     dfree(ab.coop);
     dfree(ab.heavy);
+    dfree(ab.list8);
     dfree(result);
     dfree(gpos);
     dfree(gnorm);
@@ -315,7 +316,7 @@ gbpt_status check_params(const gbpt_params* p) {
 uint64_t gbpt::renderer_bytes(uint32_t W, uint32_t H, const gbpt_params& p) {
   const size_t np = (size_t)W * H;
   const uint32_t cacheCap = std::max(1u, p.light_paths * (1 + p.light_depth_max));
-  return np * (128 + 16 + 96 + 16 + 48 + 16 + 8) + np * (12 * 10 + 4 * 2 + 4 * 4) + (size_t)cacheCap * 192;
+  return np * (128 + 16 + 96 + 16 + 48 + 16 + 8) + np * (12 * 10 + 4 * 2 + 4 * 5) + (size_t)cacheCap * 192;
 }
 
 namespace {
@@ -380,6 +381,7 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   CK(dalloc(&r->ab.filtered, np * 3));
   CK(dalloc(&r->ab.coop, kCoopWords));
   CK(dalloc(&r->ab.heavy, np));
+  CK(dalloc(&r->ab.list8, np));
   CK(cudaMemsetAsync(r->ab.coop, 0, kCoopWords * 4, r->st));
   for (float* b : {r->result, r->gpos, r->gnorm, r->gdiff, r->ab.filtered, r->gemis, r->direct, r->filtered2,
                    r->probView})

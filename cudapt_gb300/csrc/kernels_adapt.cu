@@ -12,6 +12,8 @@
 //               instead of float atomics, so the result does not depend on timing.
 #include <cuda_runtime.h>
 
+#include <cstddef>
+
 #include "gbpt_math.cuh"
 #include "launch.h"
 
@@ -301,10 +303,11 @@ __global__ void k_gen_adapt(FrameArgs a, RenderBuffers b, const uint32_t* __rest
 // slot order -- combined by a butterfly (x[l] += x[l ^ m] for m = P/2 .. 1),
 // with P = 8 for c <= 64, 32 for c <= 4096 and 1024 above.  The budget
 // spreads one frame's W*H samples very unevenly (a firefly pixel can take
-// tens of thousands), so each range has its own kernel: eight lanes per pixel
-// (four pixels per warp) for the many light pixels, a warp per pixel for the
-// medium ones, a 1024-thread CTA per pixel for the heaviest; the last two
-// take their pixels from lists the first kernel appends to.
+// tens of thousands), so each range has its own kernel: one thread per pixel
+// for c <= 8 (the same eight partials, combined in the butterfly's order),
+// eight lanes per pixel for c <= 64, a warp per pixel for the medium ones, a
+// 1024-thread CTA per pixel for the heaviest; the last three take their
+// pixels from lists the first kernel appends to.
 constexpr uint32_t kAccumSmall = 64, kAccumMid = 4096;
 constexpr uint32_t kHugeThreads = 1024;
 
@@ -360,31 +363,84 @@ __device__ __forceinline__ void accum_write(const FrameArgs& a, const RenderBuff
   sampleN[p] = N;
 }
 
-// light pixels, eight lanes each; heavier pixels are listed for the next kernels
+// The eight-lane partial of one sample (lane l holds sample l when c <= 8):
+// 0 + its contribution, or 0 when absent or infinite (accum_partials' terms)
+template <bool kMoments>
+__device__ __forceinline__ void accum_lane(const RenderBuffers& b, uint32_t s, bool present, float* v,
+                                           uint32_t& tN) {
+  for (int k = 0; k < (kMoments ? 15 : 12); k++) v[k] = 0.f;
+  if (present) accum_partials<kMoments>(b, s, 1u, 0u, 1u, v, tN);
+}
+
+template <int N>
+__device__ __forceinline__ void add_into(float* x, const float* y) {
+#pragma unroll
+  for (int k = 0; k < N; k++) x[k] = x[k] + y[k];
+}
+
+// Pixels with at most 8 samples, one thread each (most pixels of a budgeted
+// frame hold 0-2): the sum of the eight lane partials x_0..x_7 in the
+// eight-lane butterfly's order, ((x0 + x4) + (x2 + x6)) + ((x1 + x5) + (x3 +
+// x7)), so the result is that pass's to the bit.  Pixels with more samples
+// are listed for the eight-lane, warp and CTA passes.
+template <bool kMoments>
+__global__ void k_accum_one(FrameArgs a, RenderBuffers b, AdaptBuffers ab, float* result, uint32_t* sampleN,
+                            float* gpos, float* gnorm, float* gdiff) {
+  constexpr int NV = kMoments ? 15 : 12;
+  const uint32_t np = a.width * a.height;
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const uint32_t c = ab.cnt[p];
+  if (c > 8u) {
+    if (c <= kAccumSmall)
+      ab.list8[atomicAdd(&b.ctr->heavySmall, 1u)] = p;
+    else if (c <= kAccumMid)
+      ab.heavy[atomicAdd(&b.ctr->heavyMid, 1u)] = p;
+    else
+      ab.heavy[np - 1u - atomicAdd(&b.ctr->heavyHuge, 1u)] = p;
+    return;
+  }
+  const uint32_t o = c ? ab.off[p] : 0u;
+  uint32_t tN = 0;
+  float v[15], hi[NV], t[NV], u[NV];
+  // lanes {0,4} + {2,6} -> v; lanes {1,5} + {3,7} -> hi
+  const uint32_t order[2][4] = {{0u, 4u, 2u, 6u}, {1u, 5u, 3u, 7u}};
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    float* dst = h ? hi : v;
+    accum_lane<kMoments>(b, o + order[h][0], order[h][0] < c, dst, tN);
+    accum_lane<kMoments>(b, o + order[h][1], order[h][1] < c, t, tN);
+    add_into<NV>(dst, t);
+    accum_lane<kMoments>(b, o + order[h][2], order[h][2] < c, t, tN);
+    accum_lane<kMoments>(b, o + order[h][3], order[h][3] < c, u, tN);
+    add_into<NV>(t, u);
+    add_into<NV>(dst, t);
+  }
+  add_into<NV>(v, hi);
+  accum_write<kMoments>(a, b, p, v, tN, result, sampleN, gpos, gnorm, gdiff);
+}
+
+// listed pixels with 9..64 samples, eight lanes each
 template <bool kMoments>
 __global__ void k_accum(FrameArgs a, RenderBuffers b, AdaptBuffers ab, float* result, uint32_t* sampleN, float* gpos,
                         float* gnorm, float* gdiff) {
-  const uint32_t np = a.width * a.height;
-  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t p = gid >> 3, l = gid & 7u;
-  if ((gid & ~31u) >= np * 8u) return;  // whole warps past the image only
-  uint32_t c = p < np ? ab.cnt[p] : 0u;
-  if (c > kAccumSmall) {
-    if (l == 0) {
-      if (c <= kAccumMid)
-        ab.heavy[atomicAdd(&b.ctr->heavyMid, 1u)] = p;
-      else
-        ab.heavy[np - 1u - atomicAdd(&b.ctr->heavyHuge, 1u)] = p;
-    }
-    c = 0;
+  const uint32_t n = b.ctr->heavySmall;
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x, l = gid & 7u;
+  const uint32_t groups = (gridDim.x * blockDim.x) >> 3;
+  // every lane of a warp runs the same number of rounds (the shuffles need all 32)
+  const uint32_t rounds = (n + groups - 1) / groups;
+  for (uint32_t k = 0; k < rounds; k++) {
+    const uint32_t i = (gid >> 3) + k * groups;
+    const uint32_t p = i < n ? ab.list8[i] : 0u;
+    const uint32_t c = i < n ? ab.cnt[p] : 0u;
+    float v[15] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    uint32_t tN = 0;
+    if (c) accum_partials<kMoments>(b, ab.off[p], c, l, 8, v, tN);
+    for (int q = 0; q < (kMoments ? 15 : 12); q++)
+      for (int m = 4; m > 0; m >>= 1) v[q] = v[q] + __shfl_xor_sync(0xffffffffu, v[q], m);
+    for (int m = 4; m > 0; m >>= 1) tN += __shfl_xor_sync(0xffffffffu, tN, m);
+    if (l == 0 && i < n) accum_write<kMoments>(a, b, p, v, tN, result, sampleN, gpos, gnorm, gdiff);
   }
-  float v[15] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  uint32_t tN = 0;
-  if (c) accum_partials<kMoments>(b, ab.off[p], c, l, 8, v, tN);
-  for (int k = 0; k < (kMoments ? 15 : 12); k++)
-    for (int m = 4; m > 0; m >>= 1) v[k] = v[k] + __shfl_xor_sync(0xffffffffu, v[k], m);
-  for (int m = 4; m > 0; m >>= 1) tN += __shfl_xor_sync(0xffffffffu, tN, m);
-  if (l == 0 && p < np && ab.cnt[p] <= kAccumSmall) accum_write<kMoments>(a, b, p, v, tN, result, sampleN, gpos, gnorm, gdiff);
 }
 
 // medium pixels: a warp each, 32 partials
@@ -863,20 +919,23 @@ cudaError_t launch_mlp_alloc(const FrameArgs& a, const AdaptBuffers& ab, cudaStr
 cudaError_t launch_adapt_accum(const FrameArgs& a, const RenderBuffers& b, const AdaptBuffers& ab, float* result,
                                uint32_t* sampleN, float* gpos, float* gnorm, float* gdiff, cudaStream_t st) {
   const uint32_t np = a.width * a.height;
-  const uint32_t g = (uint32_t)(((size_t)np * 8 + 255) / 256);
-  cudaError_t e = cudaMemsetAsync(&b.ctr->heavyMid, 0, 2 * sizeof(uint32_t), st);
+  const uint32_t g = (np + 255) / 256;
+  static_assert(offsetof(DevCounters, heavySmall) == offsetof(DevCounters, heavyMid) + 8, "list counters");
+  cudaError_t e = cudaMemsetAsync(&b.ctr->heavyMid, 0, 3 * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   const uint32_t gm = (uint32_t)sm_count() * 8, gh = (uint32_t)sm_count();
   if (a.moments) {
-    k_accum<true><<<g, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
+    k_accum_one<true><<<g, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
+    k_accum<true><<<gm, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
     k_accum_mid<true><<<gm, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
     k_accum_huge<true><<<gh, kHugeThreads, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
   } else {
-    k_accum<false><<<g, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
+    k_accum_one<false><<<g, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
+    k_accum<false><<<gm, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
     k_accum_mid<false><<<gm, 256, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
     k_accum_huge<false><<<gh, kHugeThreads, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
   }
-  note_launches(3);
+  note_launches(4);
   return cudaGetLastError();
 }
 

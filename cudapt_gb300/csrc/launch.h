@@ -45,6 +45,7 @@ struct DevCounters {
   uint32_t fetchT;        // next ray handed to a lane by the persistent walk kernel
   uint32_t heavyMid;      // adaptive accumulation: pixels listed for the warp-per-pixel pass
   uint32_t heavyHuge;     // ... and for the CTA-per-pixel pass
+  uint32_t heavySmall;    // ... and for the eight-lanes-per-pixel pass (9..64 samples)
   unsigned long long rays, nodes, tris;  // cumulative work counters (closest-hit walks)
   unsigned long long shadowRays, nodesS, trisS;  // any-hit (shadow) walks
   double errSum;          // adaptive: sum of per-pixel errors
@@ -152,6 +153,7 @@ struct AdaptBuffers {
   float* pred;         // learned allocator: log budget weight per tile
   float* tileErr;      // learned allocator: sum of the heuristic error over each tile
   uint32_t* heavy;     // W*H: pixels with many budgeted samples (medium ones from the front, heaviest from the back)
+  uint32_t* list8;     // W*H: pixels with 9..64 budgeted samples
 };
 constexpr uint32_t kFeatures = 24;
 constexpr uint32_t kErrMlpTimeout = 256u;  // DevCounters::errFlags bit: an MLP tensor-core wait ran out

@@ -179,6 +179,11 @@ class RTRenderer:
     def handle(self):
         return self._h
 
+    def set_graphs(self, on=True):
+        """Issue each frame of the plain and PTSC modes as one CUDA graph (same image)."""
+        check(load().gbpt_renderer_set_graphs(self._h, 1 if on else 0))
+        return self
+
     def set_mlp(self, mlp=None, collect=False):
         """Learned allocation with `mlp` (cudapt_gb300.mlp.MLP) in the PLL adaptive mode;
         collect=True keeps the feature statistics without changing the allocation."""

@@ -227,6 +227,10 @@ struct gbpt_renderer {
   // current frames do not read; tag = (epoch, frame) the cache was made for
   cudaStream_t stLight = nullptr;
   cudaEvent_t evMain = nullptr, evLight[2] = {nullptr, nullptr};
+  // frames issued as CUDA graphs (plain and PTSC modes): executable graphs
+  // without / with an inline light pass
+  bool graphs = false, graphWarm = false;
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   bool lightPending[2] = {false, false};
   uint64_t epoch = 0;
   uint64_t cacheEpoch[2] = {~0ull, ~0ull};
@@ -286,6 +290,8 @@ struct gbpt_renderer {
     if (st) cudaStreamSynchronize(st);
     free_dev();
     for (auto e : evPool) cudaEventDestroy(e);
+    for (cudaGraphExec_t& x : gexec)
+      if (x) cudaGraphExecDestroy(x);
     for (cudaEvent_t e : {evMain, evLight[0], evLight[1]})
       if (e) cudaEventDestroy(e);
     if (stLight) cudaStreamDestroy(stLight);
@@ -532,6 +538,8 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   r->lastTraced = traces(r->frame);
   if (!r->lastTraced) return bilat_filter(r, st, timing);
 
+  // plain and PTSC frames can be issued as one CUDA graph (gbpt_renderer_set_graphs)
+  const bool useGraph = r->graphs && !a.counting && (r->mode == GBPT_MODE_BDPT_SC || pt);
   mark(r, kPhOther, timing);
   // light pass (src/cudaRTBDPTStream.cu:875-906): group g = frame / light_every
   // reads cache g % 2.  Its light pass normally ran ahead on the side stream;
@@ -539,101 +547,161 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   const uint32_t k = r->p.light_every;
   const uint32_t g = r->frame / k;
   const uint32_t sel = g & 1u;
+  const uint32_t nsel = sel ^ 1u;
   a.cacheSel = sel;
   r->lastSel = sel;
+  bool inlineLight = false, ahead = false;
   if (!pt && r->frame % k == 0) {
     const bool ready = r->cacheEpoch[sel] == r->epoch && r->cacheFrame[sel] == r->frame;
     if (r->lightPending[sel]) CK(cudaStreamWaitEvent(st, r->evLight[sel], 0));
     r->lightPending[sel] = false;
+    inlineLight = !ready;
     if (!ready) {
-      CK(launch_light_pass(S, a, r->rb, st));
       r->cacheEpoch[sel] = r->epoch;
       r->cacheFrame[sel] = r->frame;
+    }
+    ahead = traces(r->frame + k);
+  }
+  // the next group's light pass, ahead, into the other cache: it waits for
+  // everything queued so far (earlier frames that read that cache)
+  auto launch_ahead = [&]() -> gbpt_status {
+    CK(cudaEventRecord(r->evMain, st));
+    CK(cudaStreamWaitEvent(r->stLight, r->evMain, 0));
+    FrameArgs an = a;
+    an.frame = r->frame + k;
+    an.cacheSel = nsel;
+    CK(launch_light_pass(S, an, r->rb, r->stLight));
+    CK(cudaEventRecord(r->evLight[nsel], r->stLight));
+    r->lightPending[nsel] = true;
+    r->cacheEpoch[nsel] = r->epoch;
+    r->cacheFrame[nsel] = r->frame + k;
+    return GBPT_OK;
+  };
+  // camera rays (or the adaptive budget), the bounce loop, accumulation;
+  // tm: phase events between the launches
+  auto body = [&](bool tm) -> gbpt_status {
+    const bool budgeted = adaptive && r->frame >= r->p.warmup_frames;
+    if (budgeted) {
+      float delta = r->p.filter_sigma_spatial > 0.f ? r->p.filter_sigma_spatial : r->p.filter_color_eud;
+      gbpt_status ge = ensure_gauss(r, delta, r->p.filter_radius, st);
+      if (ge != GBPT_OK) return ge;
+      CK(launch_bilateral(r->result, r->gpos, r->gnorm, r->p.filter_diffuse ? r->gdiff : nullptr, r->W, r->H,
+                          r->p.filter_color_eud, r->p.filter_pos_eud, r->p.filter_norm_eud, r->p.filter_diff_eud,
+                          r->p.filter_radius, r->gauss, r->ab.filtered, st));
+      mark(r, kPhFilter, tm);
+      if (binary)
+        CK(launch_binary_budget(a, r->rb, r->ab, r->result, r->sampleN, r->p.desired_n, r->p.min_trace_prob, st));
+      else if (learned) {  // heuristic error -> tile features -> MLP -> per-pixel weights -> budget
+        CK(launch_adapt_error(a, r->ab, r->result, r->sampleN, r->p.desired_n, st));
+        CK(launch_tile_features(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
+        const uint32_t nTiles = a.tilesX * ((r->H + 7) / 8);
+        gbpt_status ms = mlp_forward_async(r->mlp, r->ab.feat, nTiles, r->ab.pred, &r->rb.ctr->errFlags,
+                                           kErrMlpTimeout, st);
+        if (ms != GBPT_OK) return ms;
+        CK(launch_mlp_alloc(a, r->ab, st));
+        CK(launch_adapt_alloc(a, r->rb, r->ab, st));
+      } else
+        CK(launch_adapt_budget(a, r->rb, r->ab, r->result, r->sampleN, r->p.desired_n, st));
+      mark(r, kPhAdapt, tm);
+    } else {
+      CK(launch_camera(a, r->rb, st));
+      mark(r, kPhOther, tm);
+    }
+    // bounce d < K: walk (extension rays of d + shadow rays of d-1), then shade
+    // d, one launch each; bounces >= K: one persistent kernel per frame carries
+    // every remaining path to its end (few paths are left by then, and per-bounce
+    // launches would each wait for their slowest ray)
+    int in = 0;
+    const uint32_t D = a.eyeDepth;
+    const uint32_t K = std::min(tail_from(D, S.traversal == 1 && S.wide, r->p.tail_from), D);
+    for (uint32_t d = 0; d < K; d++) {
+      CK(launch_walk(S, a, r->rb, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), d == 1, st));
+      mark(r, kPhTrace, tm);
+      CK(launch_shade(S, a, r->rb, in, d, K < D && d + 1 == K, st));
+      mark(r, kPhShade, tm);
+      in ^= 1;
+    }
+    if (K < D) {
+      CK(launch_tail(S, a, r->rb, in, K > 0 ? (int)((K - 1) & 1u) : -1, K, st));
+    } else {
+      // shadow rays of the last bounce (none in practice: paths at the depth cap
+      // terminate without connecting; kept so the sequence needs no special case)
+      CK(launch_walk(S, a, r->rb, -1, (int)((D - 1) & 1u), (int)(D & 1u), D == 1, st));
+    }
+    mark(r, kPhTrace, tm);
+    if (budgeted) {
+      if (binary)
+        CK(launch_binary_apply(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
+      else
+        CK(launch_adapt_accum(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
+      mark(r, kPhAdapt, tm);
+    } else if (pt) {
+      CK(launch_apply_pt(a, r->rb, r->result, r->sampleN, st));
+      mark(r, kPhOther, tm);
+    } else if (bilat) {
+      CK(launch_apply_bilat(a, r->rb, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, r->gemis, r->direct, r->pot,
+                            st));
+      mark(r, kPhOther, tm);
+      return bilat_filter(r, st, tm);
+    } else {
+      CK(launch_apply(a, r->rb, r->result, r->sampleN, adaptive ? r->gpos : nullptr, r->gnorm, r->gdiff, st));
+      mark(r, kPhOther, tm);
+    }
+    return GBPT_OK;
+  };
+
+  if (!useGraph || !r->graphWarm) {
+    if (inlineLight) {
+      CK(launch_light_pass(S, a, r->rb, st));
       mark(r, kPhLight, timing);
     }
-    // run the next group's light pass ahead, into the other cache: it waits
-    // for everything queued so far (earlier frames that read that cache)
-    const uint32_t nsel = sel ^ 1u;
-    if (traces(r->frame + k)) {
-      CK(cudaEventRecord(r->evMain, st));
-      CK(cudaStreamWaitEvent(r->stLight, r->evMain, 0));
-      FrameArgs an = a;
-      an.frame = r->frame + k;
-      an.cacheSel = nsel;
-      CK(launch_light_pass(S, an, r->rb, r->stLight));
-      CK(cudaEventRecord(r->evLight[nsel], r->stLight));
-      r->lightPending[nsel] = true;
-      r->cacheEpoch[nsel] = r->epoch;
-      r->cacheFrame[nsel] = r->frame + k;
+    if (ahead) {
+      gbpt_status e = launch_ahead();
+      if (e != GBPT_OK) return e;
+    }
+    if (useGraph) {  // kernels load and launch shapes are queried on first use: outside any capture
+      prepare_launches();
+      r->graphWarm = true;
+    }
+    return body(timing);
+  }
+  // One graph per frame: captured, then applied to the renderer's executable
+  // graph of the same shape (with or without an inline light pass) by
+  // cudaGraphExecUpdate, which keeps the instantiation when only kernel
+  // arguments changed.  The light pass ahead is issued after the frame.
+  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  gbpt_status bs = GBPT_OK;
+  if (inlineLight) {
+    const cudaError_t le = launch_light_pass(S, a, r->rb, st);
+    if (le != cudaSuccess) bs = fail(GBPT_ERR_CUDA, std::string("light pass: ") + cudaGetErrorString(le));
+  }
+  if (bs == GBPT_OK) bs = body(false);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+  if (bs != GBPT_OK || ce != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    if (bs != GBPT_OK) return bs;
+    return fail(GBPT_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
+  }
+  cudaGraphExec_t& ex = r->gexec[inlineLight ? 1 : 0];
+  if (ex) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(ex, graph, &info) != cudaSuccess) {
+      cudaGetLastError();
+      cudaGraphExecDestroy(ex);
+      ex = nullptr;
     }
   }
-  const bool budgeted = adaptive && r->frame >= r->p.warmup_frames;
-  if (budgeted) {
-    float delta = r->p.filter_sigma_spatial > 0.f ? r->p.filter_sigma_spatial : r->p.filter_color_eud;
-    gbpt_status ge = ensure_gauss(r, delta, r->p.filter_radius, st);
-    if (ge != GBPT_OK) return ge;
-    CK(launch_bilateral(r->result, r->gpos, r->gnorm, r->p.filter_diffuse ? r->gdiff : nullptr, r->W, r->H,
-                        r->p.filter_color_eud, r->p.filter_pos_eud, r->p.filter_norm_eud, r->p.filter_diff_eud,
-                        r->p.filter_radius, r->gauss, r->ab.filtered, st));
-    mark(r, kPhFilter, timing);
-    if (binary)
-      CK(launch_binary_budget(a, r->rb, r->ab, r->result, r->sampleN, r->p.desired_n, r->p.min_trace_prob, st));
-    else if (learned) {  // heuristic error -> tile features -> MLP -> per-pixel weights -> budget
-      CK(launch_adapt_error(a, r->ab, r->result, r->sampleN, r->p.desired_n, st));
-      CK(launch_tile_features(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
-      const uint32_t nTiles = a.tilesX * ((r->H + 7) / 8);
-      gbpt_status ms = mlp_forward_async(r->mlp, r->ab.feat, nTiles, r->ab.pred, &r->rb.ctr->errFlags,
-                                         kErrMlpTimeout, st);
-      if (ms != GBPT_OK) return ms;
-      CK(launch_mlp_alloc(a, r->ab, st));
-      CK(launch_adapt_alloc(a, r->rb, r->ab, st));
-    } else
-      CK(launch_adapt_budget(a, r->rb, r->ab, r->result, r->sampleN, r->p.desired_n, st));
-    mark(r, kPhAdapt, timing);
-  } else {
-    CK(launch_camera(a, r->rb, st));
-    mark(r, kPhOther, timing);
+  cudaError_t ie = cudaSuccess;
+  if (!ex) ie = cudaGraphInstantiate(&ex, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess) {
+    ex = nullptr;
+    return fail(GBPT_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
   }
-  // bounce d < K: walk (extension rays of d + shadow rays of d-1), then shade
-  // d, one launch each; bounces >= K: one persistent kernel per frame carries
-  // every remaining path to its end (few paths are left by then, and per-bounce
-  // launches would each wait for their slowest ray)
-  int in = 0;
-  const uint32_t D = a.eyeDepth;
-  const uint32_t K = std::min(tail_from(D, S.traversal == 1 && S.wide, r->p.tail_from), D);
-  for (uint32_t d = 0; d < K; d++) {
-    CK(launch_walk(S, a, r->rb, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), d == 1, st));
-    mark(r, kPhTrace, timing);
-    CK(launch_shade(S, a, r->rb, in, d, K < D && d + 1 == K, st));
-    mark(r, kPhShade, timing);
-    in ^= 1;
-  }
-  if (K < D) {
-    CK(launch_tail(S, a, r->rb, in, K > 0 ? (int)((K - 1) & 1u) : -1, K, st));
-  } else {
-    // shadow rays of the last bounce (none in practice: paths at the depth cap
-    // terminate without connecting; kept so the sequence needs no special case)
-    CK(launch_walk(S, a, r->rb, -1, (int)((D - 1) & 1u), (int)(D & 1u), D == 1, st));
-  }
+  CK(cudaGraphLaunch(ex, st));
   mark(r, kPhTrace, timing);
-  if (budgeted) {
-    if (binary)
-      CK(launch_binary_apply(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
-    else
-      CK(launch_adapt_accum(a, r->rb, r->ab, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, st));
-    mark(r, kPhAdapt, timing);
-  } else if (pt) {
-    CK(launch_apply_pt(a, r->rb, r->result, r->sampleN, st));
-    mark(r, kPhOther, timing);
-  } else if (bilat) {
-    CK(launch_apply_bilat(a, r->rb, r->result, r->sampleN, r->gpos, r->gnorm, r->gdiff, r->gemis, r->direct, r->pot,
-                          st));
-    mark(r, kPhOther, timing);
-    return bilat_filter(r, st, timing);
-  } else {
-    CK(launch_apply(a, r->rb, r->result, r->sampleN, adaptive ? r->gpos : nullptr, r->gnorm, r->gdiff, st));
-    mark(r, kPhOther, timing);
-  }
+  if (ahead) return launch_ahead();
   return GBPT_OK;
 }
 
@@ -1167,6 +1235,12 @@ gbpt_status gbpt_renderer_set_stream(gbpt_renderer* r, void* stream) {
   if (!r->ownSt) r->ownSt = r->st;
   r->st = stream ? (cudaStream_t)stream : r->ownSt;
   r->userStream = stream != nullptr;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_renderer_set_graphs(gbpt_renderer* r, int32_t on) {
+  if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
+  r->graphs = on != 0;
   return GBPT_OK;
 }
 

@@ -915,17 +915,35 @@ cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream
   return cudaGetLastError();
 }
 
+// launch shapes, queried once per kernel
+template <bool kCount, bool kWide>
+uint32_t walk_grid() {
+  static uint32_t g = grid_for((const void*)k_walk<kCount, kWide>);
+  return g;
+}
+
+template <bool kCount, bool kWide>
+uint32_t tail_grid() {
+  static uint32_t g = grid_for((const void*)k_tail<kCount, kWide>);
+  return g;
+}
+
+uint32_t shade_grid() {
+  static uint32_t g = grid_for((const void*)k_shade);
+  return g;
+}
+
 template <bool kCount, bool kWide>
 void walk_variant(const DevScene& S, const RenderBuffers& b, int in, int shIn, int shReset, uint32_t sd,
                   uint32_t refill, cudaStream_t st) {
-  static uint32_t g = grid_for((const void*)k_walk<kCount, kWide>);
+  const uint32_t g = walk_grid<kCount, kWide>();
   k_walk<kCount, kWide><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, sd, refill);
 }
 
 template <bool kCount, bool kWide>
 void tail_variant(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn, uint32_t depth0,
                   cudaStream_t st) {
-  static uint32_t g = grid_for((const void*)k_tail<kCount, kWide>);
+  const uint32_t g = tail_grid<kCount, kWide>();
   k_tail<kCount, kWide><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill_for(a.refill));
 }
 
@@ -959,6 +977,18 @@ cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffe
   return cudaGetLastError();
 }
 
+void prepare_launches() {
+  walk_grid<false, false>();
+  walk_grid<false, true>();
+  walk_grid<true, false>();
+  walk_grid<true, true>();
+  tail_grid<false, false>();
+  tail_grid<false, true>();
+  tail_grid<true, false>();
+  tail_grid<true, true>();
+  shade_grid();
+}
+
 uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested) {
   // default, reference order: the last 4 bounces (measured on the 1024x768
   // interior, depth 10: the tail kernel from bounce 6 beats both per-bounce
@@ -981,7 +1011,7 @@ uint32_t walk_refill_for(uint32_t requested) {
 
 cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t depth,
                          bool attach, cudaStream_t st) {
-  static uint32_t g = grid_for((const void*)k_shade);
+  const uint32_t g = shade_grid();
   k_shade<<<g, kBlock, 0, st>>>(S, a, b, in, depth, attach ? 1u : 0u);
   note_launches(1);
   return cudaGetLastError();

@@ -122,6 +122,9 @@ uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested);
 // refill threshold of the persistent walks: `requested` when 1..32, else
 // GBPT_WALK_REFILL when set, else 20
 uint32_t walk_refill_for(uint32_t requested);
+// Queries (once) the launch shapes of the wavefront kernels, which also loads
+// them: call before the first stream capture.
+void prepare_launches();
 cudaError_t launch_apply(const FrameArgs& a, const RenderBuffers& b, float* result, uint32_t* sampleN, float* gpos,
                          float* gnorm, float* gdiff, cudaStream_t st);
 // filter-only mode (src/cudaRTBDPTStreamBilat.cu:989-1051): running means of

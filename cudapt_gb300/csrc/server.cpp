@@ -139,6 +139,7 @@ struct gbpt_server {
   bool stop = false;
   int device = 0;
   int32_t policy = GBPT_SERVE_SHORTEST_FIRST;
+  bool graphs = false;  // renderers issue plain / PTSC frames as CUDA graphs
 
   ~gbpt_server() {
     {
@@ -272,6 +273,7 @@ static gbpt_status run_request(gbpt_server* srv, Pool& pool, Request& q, std::st
   }
   gbpt_status st = gbpt_set_params(r, &p);
   if (st == GBPT_OK) st = gbpt_reset(r);
+  if (st == GBPT_OK) st = gbpt_renderer_set_graphs(r, srv->graphs ? 1 : 0);
   gbpt_stats a{}, b{};
   if (st == GBPT_OK && q.q.frames > 1) st = gbpt_render_frames(r, q.q.scene, &q.q.camera, q.q.frames - 1, &a);
   if (st == GBPT_OK && q.q.frames > 0) st = gbpt_render(r, q.q.scene, &q.q.camera, q.q.out_rgb, 0, &b);
@@ -352,6 +354,13 @@ gbpt_status gbpt_server_set_policy(gbpt_server* s, int32_t policy) {
     return fail(GBPT_ERR_INVALID_ARG, "unknown queue policy");
   std::lock_guard<std::mutex> lock(s->mu);
   s->policy = policy;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_server_set_graphs(gbpt_server* s, int32_t on) {
+  if (!s) return fail(GBPT_ERR_INVALID_ARG, "server is NULL");
+  std::lock_guard<std::mutex> lock(s->mu);
+  s->graphs = on != 0;
   return GBPT_OK;
 }
 

@@ -31,12 +31,13 @@ class Server:
 
     FIFO, SHORTEST_FIRST = 0, 1
 
-    def __init__(self, workers=4, hbm_reserve=1 << 30, policy=SHORTEST_FIRST):
+    def __init__(self, workers=4, hbm_reserve=1 << 30, policy=SHORTEST_FIRST, graphs=False):
         h = ctypes.c_void_p()
         check(load().gbpt_server_create(int(workers), int(hbm_reserve), ctypes.addressof(h)))
         self._h = h
         self._keep = {}  # id -> objects the library reads until the request ends
         check(load().gbpt_server_set_policy(self._h, int(policy)))
+        check(load().gbpt_server_set_graphs(self._h, 1 if graphs else 0))
 
     def submit(self, scene, cam, width, height, frames, mode=layouts.MODE_BDPT_SC, params=None, out=None):
         """Queue one request; `out` (float32, width*height*3, optional) receives the image.
@@ -108,13 +109,13 @@ def poisson_workload(n=64, rate=200.0, seed=0, scenes=("cornell", "interior", "h
 
 
 def run_poisson(gb, workload, scene_objs, cameras, workers=4, hbm_reserve=1 << 30, warm=True,
-                policy=Server.SHORTEST_FIRST):
+                policy=Server.SHORTEST_FIRST, graphs=False):
     """Submit `workload` (from poisson_workload) at its arrival times.  Scenes
     are built and resident beforehand; result buffers are page-locked before
     the clock starts.  Returns a summary dict and the per-request statuses."""
     from . import _host_floats
     bufs = [_host_floats(w * h * 3) for (_, _, w, h, _, _) in workload]
-    srv = Server(workers, hbm_reserve, policy)
+    srv = Server(workers, hbm_reserve, policy, graphs)
     try:
         if warm:  # first-use costs (kernel loading, scene upload) outside the timed run
             ids = [srv.submit(scene_objs[name], cameras[name], 64, 64, 1,
@@ -149,5 +150,6 @@ def run_poisson(gb, workload, scene_objs, cameras, workers=4, hbm_reserve=1 << 3
         "mpaths_per_s": round(paths / wall / 1e6, 3),
         "workers": workers,
         "policy": "shortest first (aging)" if policy == Server.SHORTEST_FIRST else "fifo",
+        "graphs": bool(graphs),
     }
     return summary, st

@@ -309,6 +309,11 @@ gbpt_status gbpt_mlp_train_step(gbpt_mlp* m, const float* x, const float* t, uin
  * stream), so that several renderers can be batched on streams the caller
  * schedules.  Every call still returns when its frame is complete. */
 gbpt_status gbpt_renderer_set_stream(gbpt_renderer* r, void* stream);
+/* on != 0: in the plain (BDPT_SC) and PTSC modes each frame's launches are
+ * captured and issued as one CUDA graph (updated in place from frame to
+ * frame); the image is the same.  With stats, only ms_total is broken down
+ * (into the trace phase).  Off by default. */
+gbpt_status gbpt_renderer_set_graphs(gbpt_renderer* r, int32_t on);
 
 /* Learned allocation in GBPT_MODE_BDPT_SC_ADAP_BILAT: with mlp != NULL every
  * budgeted frame turns the heuristic per-pixel error into per-tile weights
@@ -367,6 +372,9 @@ gbpt_status gbpt_server_create(uint32_t workers, uint64_t hbm_reserve_bytes, gbp
  * 1e5 paths per ms) minus the time it has waited starts next. */
 enum { GBPT_SERVE_FIFO = 0, GBPT_SERVE_SHORTEST_FIRST = 1 };
 gbpt_status gbpt_server_set_policy(gbpt_server* s, int32_t policy);
+/* on != 0: the server's renderers issue plain / PTSC frames as CUDA graphs
+ * (gbpt_renderer_set_graphs). */
+gbpt_status gbpt_server_set_graphs(gbpt_server* s, int32_t on);
 /* Finishes the queued and running requests, then frees every renderer. */
 gbpt_status gbpt_server_destroy(gbpt_server* s);
 gbpt_status gbpt_server_submit(gbpt_server* s, const gbpt_request* req, uint64_t* id);

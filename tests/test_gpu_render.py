@@ -282,3 +282,32 @@ def test_full_size_frame_bands_match_oracle(gbdev, orc, name, W, H, depth):
         same = np.mean(got.view(np.uint32) == want.view(np.uint32))
         assert same >= 0.995, (y0, same)
         assert abs(float(got.mean()) - float(want.mean())) <= 2e-3 * max(float(want.mean()), 1e-6)
+
+
+@pytest.mark.parametrize("mode,depth", [(0, 10), (4, 8)])
+def test_graph_frames_equal_direct_launches(gbdev, mode, depth):
+    """Frames issued as CUDA graphs (plain and PTSC) give the images of direct
+    launches: across light-pass frames, a camera change and knob changes that
+    alter the graph's shape (tail kernel or not)."""
+    (v, t, m), cam = scene_arrays("interior")
+    s = gbdev.RTScene(v, t, m).build_bvh()
+    cam2 = dict(cam)
+    cam2["pos"] = [float(x) + 0.25 for x in cam["pos"]]
+    p = gbdev.default_params(eye_depth_max=depth, light_depth_max=depth, pt_depth_max=depth)
+    runs = []
+    for graphs in (False, True):
+        r = gbdev.RTRenderer(80, 60, mode, p)
+        r.set_graphs(graphs)
+        imgs = []
+        for f in range(9):
+            c = cam if f < 5 else cam2
+            if f == 6:  # restarts accumulation with knobs that change the graph's shape
+                r.params = gbdev.default_params(eye_depth_max=depth, light_depth_max=depth, pt_depth_max=depth,
+                                                tail_from=depth, walk_refill=12)
+            imgs.append(r.render(s, c, stats=(f == 8)).copy())
+        runs.append(imgs)
+        if graphs:
+            assert r.last_stats["ms_total"] > 0
+        r.close()
+    for f, (a, b) in enumerate(zip(*runs)):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), f

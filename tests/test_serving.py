@@ -38,8 +38,8 @@ def _alone(gb, scene, cam, w, h, frames, mode, params):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("policy", [1, 0])
-def test_server_images_equal_single_renders(gbdev, policy):
+@pytest.mark.parametrize("policy,graphs", [(1, False), (0, True)])
+def test_server_images_equal_single_renders(gbdev, policy, graphs):
     from cudapt_gb300 import serving
     (v, t, m), cam = scene_arrays("cornell")
     cornell = gbdev.RTScene(v, t, m).build_bvh()
@@ -48,7 +48,7 @@ def test_server_images_equal_single_renders(gbdev, policy):
     jobs = [(cornell, cam, 64, 48, 3, 0, 8), (interior, cam2, 96, 64, 4, 0, 10), (cornell, cam, 32, 32, 7, 1, 6),
             (interior, cam2, 80, 60, 2, 4, 8), (cornell, cam, 64, 48, 3, 0, 8), (interior, cam2, 96, 64, 5, 3, 6)]
     outs = [np.zeros(w * h * 3, np.float32) for (_, _, w, h, _, _, _) in jobs]
-    with serving.Server(workers=3, policy=policy) as srv:
+    with serving.Server(workers=3, policy=policy, graphs=graphs) as srv:
         ids = []
         for (s, c, w, h, f, mode, d), o in zip(jobs, outs):
             p = gbdev.default_params(eye_depth_max=d, light_depth_max=d, pt_depth_max=d, warmup_frames=2)

@@ -139,7 +139,7 @@ struct gbpt_server {
   bool stop = false;
   int device = 0;
   int32_t policy = GBPT_SERVE_SHORTEST_FIRST;
-  bool graphs = false;  // renderers issue plain / PTSC frames as CUDA graphs
+  bool graphs = true;  // renderers issue plain / PTSC frames as CUDA graphs
 
   ~gbpt_server() {
     {

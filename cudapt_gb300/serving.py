@@ -31,7 +31,7 @@ class Server:
 
     FIFO, SHORTEST_FIRST = 0, 1
 
-    def __init__(self, workers=4, hbm_reserve=1 << 30, policy=SHORTEST_FIRST, graphs=False):
+    def __init__(self, workers=4, hbm_reserve=1 << 30, policy=SHORTEST_FIRST, graphs=True):
         h = ctypes.c_void_p()
         check(load().gbpt_server_create(int(workers), int(hbm_reserve), ctypes.addressof(h)))
         self._h = h
@@ -109,7 +109,7 @@ def poisson_workload(n=64, rate=200.0, seed=0, scenes=("cornell", "interior", "h
 
 
 def run_poisson(gb, workload, scene_objs, cameras, workers=4, hbm_reserve=1 << 30, warm=True,
-                policy=Server.SHORTEST_FIRST, graphs=False):
+                policy=Server.SHORTEST_FIRST, graphs=True):
     """Submit `workload` (from poisson_workload) at its arrival times.  Scenes
     are built and resident beforehand; result buffers are page-locked before
     the clock starts.  Returns a summary dict and the per-request statuses."""

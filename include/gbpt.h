@@ -372,8 +372,8 @@ gbpt_status gbpt_server_create(uint32_t workers, uint64_t hbm_reserve_bytes, gbp
  * 1e5 paths per ms) minus the time it has waited starts next. */
 enum { GBPT_SERVE_FIFO = 0, GBPT_SERVE_SHORTEST_FIRST = 1 };
 gbpt_status gbpt_server_set_policy(gbpt_server* s, int32_t policy);
-/* on != 0: the server's renderers issue plain / PTSC frames as CUDA graphs
- * (gbpt_renderer_set_graphs). */
+/* on != 0 (default): the server's renderers issue plain / PTSC frames as
+ * CUDA graphs (gbpt_renderer_set_graphs). */
 gbpt_status gbpt_server_set_graphs(gbpt_server* s, int32_t on);
 /* Finishes the queued and running requests, then frees every renderer. */
 gbpt_status gbpt_server_destroy(gbpt_server* s);

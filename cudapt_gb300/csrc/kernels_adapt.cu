@@ -312,23 +312,46 @@ constexpr uint32_t kAccumSmall = 64, kAccumMid = 4096;
 constexpr uint32_t kHugeThreads = 1024;
 
 template <bool kMoments>
+__device__ __forceinline__ void accum_sample(float4 r, float4 g0, float4 g1, float4 g2, float* v, uint32_t& tN) {
+  if (isinf(r.x) || isinf(r.y) || isinf(r.z)) return;
+  uint32_t n = __float_as_uint(r.w);
+  float fn = (float)n;
+  v[0] = v[0] + r.x; v[1] = v[1] + r.y; v[2] = v[2] + r.z;
+  v[3] = v[3] + g0.x * fn; v[4] = v[4] + g0.y * fn; v[5] = v[5] + g0.z * fn;
+  v[6] = v[6] + g1.x * fn; v[7] = v[7] + g1.y * fn; v[8] = v[8] + g1.z * fn;
+  v[9] = v[9] + g2.x * fn; v[10] = v[10] + g2.y * fn; v[11] = v[11] + g2.z * fn;
+  if (kMoments) {  // second moments for the learned allocator's features
+    v[12] = v[12] + (r.x * r.x) / fn; v[13] = v[13] + (r.y * r.y) / fn; v[14] = v[14] + (r.z * r.z) / fn;
+  }
+  tN += n;
+}
+
+// Partial l of pixel samples [o, o + c): samples l, l + P, l + 2P, ... added
+// one after another in that order.  The loads of four samples are issued
+// before their additions (the order of the additions is unchanged), so a
+// lane with a long run -- a heavy pixel's warp or CTA lanes walk up to a few
+// hundred samples each -- keeps four loads in flight instead of one.
+template <bool kMoments>
 __device__ __forceinline__ void accum_partials(const RenderBuffers& b, uint32_t o, uint32_t c, uint32_t l, uint32_t P,
                                                float* v, uint32_t& tN) {
-  for (uint32_t s = o + l; s < o + c; s += P) {
-    float4 r = b.res[s];
-    if (isinf(r.x) || isinf(r.y) || isinf(r.z)) continue;
-    uint32_t n = __float_as_uint(r.w);
-    float fn = (float)n;
-    float4 g0 = b.gbuf[3 * (size_t)s], g1 = b.gbuf[3 * (size_t)s + 1], g2 = b.gbuf[3 * (size_t)s + 2];
-    v[0] = v[0] + r.x; v[1] = v[1] + r.y; v[2] = v[2] + r.z;
-    v[3] = v[3] + g0.x * fn; v[4] = v[4] + g0.y * fn; v[5] = v[5] + g0.z * fn;
-    v[6] = v[6] + g1.x * fn; v[7] = v[7] + g1.y * fn; v[8] = v[8] + g1.z * fn;
-    v[9] = v[9] + g2.x * fn; v[10] = v[10] + g2.y * fn; v[11] = v[11] + g2.z * fn;
-    if (kMoments) {  // second moments for the learned allocator's features
-      v[12] = v[12] + (r.x * r.x) / fn; v[13] = v[13] + (r.y * r.y) / fn; v[14] = v[14] + (r.z * r.z) / fn;
+  const uint32_t end = o + c;
+  uint32_t s = o + l;
+  for (; s + 3 * P < end; s += 4 * P) {
+    float4 r[4], g0[4], g1[4], g2[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const size_t q = (size_t)s + (size_t)j * P;
+      r[j] = b.res[q];
+      g0[j] = b.gbuf[3 * q];
+      g1[j] = b.gbuf[3 * q + 1];
+      g2[j] = b.gbuf[3 * q + 2];
     }
-    tN += n;
+#pragma unroll
+    for (int j = 0; j < 4; j++) accum_sample<kMoments>(r[j], g0[j], g1[j], g2[j], v, tN);
   }
+  for (; s < end; s += P)
+    accum_sample<kMoments>(b.res[s], b.gbuf[3 * (size_t)s], b.gbuf[3 * (size_t)s + 1], b.gbuf[3 * (size_t)s + 2], v,
+                           tN);
 }
 
 // running means of pixel p from its summed samples (one thread)

@@ -327,19 +327,20 @@ __device__ __forceinline__ void accum_sample(float4 r, float4 g0, float4 g1, flo
 }
 
 // Partial l of pixel samples [o, o + c): samples l, l + P, l + 2P, ... added
-// one after another in that order.  The loads of four samples are issued
+// one after another in that order.  The loads of kBatch samples are issued
 // before their additions (the order of the additions is unchanged), so a
 // lane with a long run -- a heavy pixel's warp or CTA lanes walk up to a few
-// hundred samples each -- keeps four loads in flight instead of one.
-template <bool kMoments>
+// hundred samples each -- keeps kBatch loads in flight instead of one (2 in
+// the 1024-thread kernel, whose 64 registers a thread do not hold four).
+template <bool kMoments, int kBatch = 4>
 __device__ __forceinline__ void accum_partials(const RenderBuffers& b, uint32_t o, uint32_t c, uint32_t l, uint32_t P,
                                                float* v, uint32_t& tN) {
   const uint32_t end = o + c;
   uint32_t s = o + l;
-  for (; s + 3 * P < end; s += 4 * P) {
-    float4 r[4], g0[4], g1[4], g2[4];
+  for (; s + (kBatch - 1) * P < end; s += kBatch * P) {
+    float4 r[kBatch], g0[kBatch], g1[kBatch], g2[kBatch];
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < kBatch; j++) {
       const size_t q = (size_t)s + (size_t)j * P;
       r[j] = b.res[q];
       g0[j] = b.gbuf[3 * q];
@@ -347,7 +348,7 @@ __device__ __forceinline__ void accum_partials(const RenderBuffers& b, uint32_t 
       g2[j] = b.gbuf[3 * q + 2];
     }
 #pragma unroll
-    for (int j = 0; j < 4; j++) accum_sample<kMoments>(r[j], g0[j], g1[j], g2[j], v, tN);
+    for (int j = 0; j < kBatch; j++) accum_sample<kMoments>(r[j], g0[j], g1[j], g2[j], v, tN);
   }
   for (; s < end; s += P)
     accum_sample<kMoments>(b.res[s], b.gbuf[3 * (size_t)s], b.gbuf[3 * (size_t)s + 1], b.gbuf[3 * (size_t)s + 2], v,
@@ -392,7 +393,9 @@ template <bool kMoments>
 __device__ __forceinline__ void accum_lane(const RenderBuffers& b, uint32_t s, bool present, float* v,
                                            uint32_t& tN) {
   for (int k = 0; k < (kMoments ? 15 : 12); k++) v[k] = 0.f;
-  if (present) accum_partials<kMoments>(b, s, 1u, 0u, 1u, v, tN);
+  if (present)
+    accum_sample<kMoments>(b.res[s], b.gbuf[3 * (size_t)s], b.gbuf[3 * (size_t)s + 1], b.gbuf[3 * (size_t)s + 2], v,
+                           tN);
 }
 
 template <int N>
@@ -499,7 +502,7 @@ __global__ void __launch_bounds__(kHugeThreads) k_accum_huge(FrameArgs a, Render
     const uint32_t p = ab.heavy[np - 1u - h];
     float v[15] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     uint32_t tN = 0;
-    accum_partials<kMoments>(b, ab.off[p], ab.cnt[p], t, kHugeThreads, v, tN);
+    accum_partials<kMoments, 2>(b, ab.off[p], ab.cnt[p], t, kHugeThreads, v, tN);
     for (int k = 0; k < (kMoments ? 15 : 12); k++) {
       float x = v[k];
       for (uint32_t m = kHugeThreads / 2; m >= 32; m >>= 1) {

@@ -120,6 +120,7 @@ SIGNATURES = {
     "gbpt_server_create": (i32, [u32, ctypes.c_uint64, vp]),
     "gbpt_server_destroy": (i32, [vp]),
     "gbpt_server_set_policy": (i32, [vp, i32]),
+    "gbpt_server_release": (i32, [vp, ctypes.c_uint64]),
     "gbpt_server_set_graphs": (i32, [vp, i32]),
     "gbpt_renderer_set_graphs": (i32, [vp, i32]),
     "gbpt_server_submit": (i32, [vp, vp, vp]),

@@ -421,6 +421,16 @@ gbpt_status gbpt_server_wait(gbpt_server* s, uint64_t id, uint32_t timeout_ms, g
   return GBPT_OK;
 }
 
+gbpt_status gbpt_server_release(gbpt_server* s, uint64_t id) {
+  if (!s) return fail(GBPT_ERR_INVALID_ARG, "server is NULL");
+  std::lock_guard<std::mutex> lock(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return fail(GBPT_ERR_INVALID_ARG, "unknown request id");
+  if (!it->second->done) return fail(GBPT_ERR_STATE, "request still queued or running");
+  s->reqs.erase(it);
+  return GBPT_OK;
+}
+
 gbpt_status gbpt_server_tuned(gbpt_server* s, int32_t mode, uint32_t depth, uint32_t width, uint32_t height,
                               uint32_t* walk_refill, int32_t* tail_from, uint32_t* samples) {
   if (!s || !walk_refill || !tail_from || !samples) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");

@@ -60,11 +60,14 @@ class Server:
         self._keep[rid.value] = (scene, out)
         return rid.value
 
-    def wait(self, rid, timeout_ms=600_000):
-        """Status of request `rid` once finished (raises GbptError on timeout)."""
+    def wait(self, rid, timeout_ms=600_000, release=True):
+        """Status of request `rid` once finished (raises GbptError on timeout);
+        release: let the server forget it afterwards."""
         st = RequestStatus()
         check(load().gbpt_server_wait(self._h, int(rid), int(timeout_ms), ctypes.addressof(st)))
         self._keep.pop(int(rid), None)
+        if release:
+            check(load().gbpt_server_release(self._h, int(rid)))
         return st.as_dict()
 
     def tuned(self, mode, depth, width, height):

@@ -382,6 +382,9 @@ gbpt_status gbpt_server_submit(gbpt_server* s, const gbpt_request* req, uint64_t
  * is still queued or running (out->done = 0).  A finished request's status
  * stays readable until the server is destroyed. */
 gbpt_status gbpt_server_wait(gbpt_server* s, uint64_t id, uint32_t timeout_ms, gbpt_request_status* out);
+/* Forgets a finished request's status (a long-running server otherwise keeps
+ * every status until it is destroyed); GBPT_ERR_STATE while it runs. */
+gbpt_status gbpt_server_release(gbpt_server* s, uint64_t id);
 /* The autotuner's choice for a class: *samples requests timed so far. */
 gbpt_status gbpt_server_tuned(gbpt_server* s, int32_t mode, uint32_t depth, uint32_t width, uint32_t height,
                               uint32_t* walk_refill, int32_t* tail_from, uint32_t* samples);

@@ -88,6 +88,12 @@ def test_server_autotuner_and_admission(gbdev):
         refill, tail, n = srv.tuned(0, 5, 64, 64)
         assert n == 16 and refill in (12, 20, 28) and tail in (-1, 2, 5)
         assert len({(r["walk_refill"], r["tail_from"]) for r in st}) >= 3  # candidates were explored
+    # a released status is gone
+    with serving.Server(workers=1) as srv:
+        rid = srv.submit(s, cam, 32, 32, 1)
+        assert srv.wait(rid)["status"] == 0
+        with pytest.raises(gbdev.GbptError):
+            srv.wait(rid, timeout_ms=0)
     # a reserve larger than the device: nothing can be admitted, and nothing else runs
     with serving.Server(workers=1, hbm_reserve=1 << 50) as srv:
         r = srv.wait(srv.submit(s, cam, 64, 64, 1))

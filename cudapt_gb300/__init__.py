@@ -179,6 +179,22 @@ class RTRenderer:
     def handle(self):
         return self._h
 
+    def checkpoint(self):
+        """The renderer's whole progressive state as bytes (gbpt_renderer_checkpoint)."""
+        n = ctypes.c_size_t()
+        check(load().gbpt_renderer_checkpoint_size(self._h, ctypes.addressof(n)))
+        buf = np.empty(n.value, np.uint8)
+        check(load().gbpt_renderer_checkpoint(self._h, ptr(buf), buf.nbytes))
+        return buf.tobytes()
+
+    def restore(self, data):
+        """Continue from checkpoint() bytes: the next render with the same scene and
+        camera gives the frame the interrupted renderer would have given."""
+        buf = np.frombuffer(data, np.uint8)
+        check(load().gbpt_renderer_restore(self._h, ptr(buf), buf.nbytes))
+        self._mode = int(np.frombuffer(data[20:24], np.int32)[0])  # the header's mode word
+        return self
+
     def set_graphs(self, on=True):
         """Issue each frame of the plain and PTSC modes as one CUDA graph (same image)."""
         check(load().gbpt_renderer_set_graphs(self._h, 1 if on else 0))

@@ -233,6 +233,11 @@ struct gbpt_renderer {
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   bool lightPending[2] = {false, false};
   uint64_t epoch = 0;
+  // a restored checkpoint adopts the next frame's scene when it has the
+  // checkpoint's triangle and node counts (scene handles do not outlive a process)
+  bool resumeScene = false;
+  uint32_t resumeTriN = 0, resumeNodeN = 0;
+  uint32_t lastTriN = 0, lastNodeN = 0;  // the scene of the last frame (checkpoint check)
   uint64_t cacheEpoch[2] = {~0ull, ~0ull};
   uint32_t cacheFrame[2] = {0, 0};
   uint32_t lastSel = 0;
@@ -485,12 +490,20 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   cam_basis(*cam, right, up);
   float basis9[9] = {cam->pos[0], cam->pos[1], cam->pos[2], cam->dir[0], cam->dir[1],
                      cam->dir[2], up[0],       up[1],       up[2]};
+  if (r->resumeScene) {
+    if (s->dev.triN != r->resumeTriN || s->bvh.nodeN != r->resumeNodeN)
+      return fail(GBPT_ERR_STATE, "the checkpoint was made with another scene");
+    r->sceneVersion = s->version;
+    r->resumeScene = false;
+  }
   bool same = r->started && r->sceneVersion == s->version && std::memcmp(basis9, r->camBasis, sizeof(basis9)) == 0;
   r->frame = same ? r->frame + 1 : 0;
   if (!same) r->epoch++;  // light passes made ahead for the old sequence are stale
   std::memcpy(r->camBasis, basis9, sizeof(basis9));
   r->started = true;
   r->sceneVersion = s->version;
+  r->lastTriN = s->dev.triN;
+  r->lastNodeN = s->bvh.nodeN;
 
   FrameArgs a{};
   for (int k = 0; k < 3; k++) {
@@ -551,16 +564,21 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   a.cacheSel = sel;
   r->lastSel = sel;
   bool inlineLight = false, ahead = false;
-  if (!pt && r->frame % k == 0) {
-    const bool ready = r->cacheEpoch[sel] == r->epoch && r->cacheFrame[sel] == r->frame;
+  // the group's first frame: its light pass (a frame inside a group whose
+  // cache is not there -- after a restored checkpoint -- makes it too)
+  const uint32_t g0 = r->frame - r->frame % k;
+  FrameArgs al = a;
+  al.frame = g0;
+  if (!pt && (r->frame == g0 || r->cacheEpoch[sel] != r->epoch || r->cacheFrame[sel] != g0)) {
+    const bool ready = r->cacheEpoch[sel] == r->epoch && r->cacheFrame[sel] == g0;
     if (r->lightPending[sel]) CK(cudaStreamWaitEvent(st, r->evLight[sel], 0));
     r->lightPending[sel] = false;
     inlineLight = !ready;
     if (!ready) {
       r->cacheEpoch[sel] = r->epoch;
-      r->cacheFrame[sel] = r->frame;
+      r->cacheFrame[sel] = g0;
     }
-    ahead = traces(r->frame + k);
+    ahead = r->frame == g0 && traces(r->frame + k);
   }
   // the next group's light pass, ahead, into the other cache: it waits for
   // everything queued so far (earlier frames that read that cache)
@@ -652,7 +670,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
 
   if (!useGraph || !r->graphWarm) {
     if (inlineLight) {
-      CK(launch_light_pass(S, a, r->rb, st));
+      CK(launch_light_pass(S, al, r->rb, st));
       mark(r, kPhLight, timing);
     }
     if (ahead) {
@@ -672,7 +690,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   gbpt_status bs = GBPT_OK;
   if (inlineLight) {
-    const cudaError_t le = launch_light_pass(S, a, r->rb, st);
+    const cudaError_t le = launch_light_pass(S, al, r->rb, st);
     if (le != cudaSuccess) bs = fail(GBPT_ERR_CUDA, std::string("light pass: ") + cudaGetErrorString(le));
   }
   if (bs == GBPT_OK) bs = body(false);
@@ -1279,6 +1297,120 @@ gbpt_status gbpt_renderer_features(gbpt_renderer* r, float* out, uint32_t capaci
   CK(cudaMemcpyAsync(out, r->ab.feat, (size_t)nTiles * kFeatures * 4,
                      out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  return GBPT_OK;
+}
+
+// ---- checkpoint / resume ---------------------------------------------------
+// Layout: CkHeader, then the device planes of ck_planes() in order.  Every
+// random number of a frame follows from (seed, request id, frame, pixel,
+// sample), so the accumulators, the sample counts and the frame counter are
+// the whole state: a restored renderer continues the interrupted sequence to
+// the bit (the light cache of the current group is made again on the next
+// frame).
+namespace {
+
+struct CkHeader {
+  char magic[8];  // "GBPTCKP1"
+  uint32_t version, W, H;
+  int32_t mode;
+  uint32_t frame, started, bilatIs2, triN, nodeN;
+  float camBasis[9];
+  float debugMode;
+  gbpt_params p;
+};
+
+struct CkPlane {
+  void* dev;
+  size_t bytes;
+};
+
+std::vector<CkPlane> ck_planes(gbpt_renderer* r) {
+  const size_t np = (size_t)r->W * r->H;
+  const size_t nTiles = (size_t)((r->W + 7) / 8) * ((r->H + 7) / 8);
+  return {{r->result, np * 12},     {r->sampleN, np * 4},   {r->gpos, np * 12},        {r->gnorm, np * 12},
+          {r->gdiff, np * 12},      {r->gemis, np * 12},    {r->direct, np * 12},      {r->pot, np * 4},
+          {r->filtered2, np * 12},  {r->probView, np * 12}, {r->ab.filtered, np * 12}, {r->rb.m2, np * 12},
+          {r->rb.hist, nTiles * 32}};
+}
+
+size_t ck_bytes(gbpt_renderer* r) {
+  size_t n = sizeof(CkHeader);
+  const size_t np = (size_t)r->W * r->H;
+  const size_t nTiles = (size_t)((r->W + 7) / 8) * ((r->H + 7) / 8);
+  n += np * (12 * 11 + 4 * 2) + nTiles * 32;
+  return n;
+}
+
+}  // namespace
+
+gbpt_status gbpt_renderer_checkpoint_size(gbpt_renderer* r, size_t* bytes) {
+  if (!r || !bytes) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  *bytes = ck_bytes(r);
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_renderer_checkpoint(gbpt_renderer* r, void* buf, size_t bytes) {
+  if (!r || !buf) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  if (bytes < ck_bytes(r)) return fail(GBPT_ERR_INVALID_ARG, "checkpoint buffer too small");
+  if (!r->alloc || !r->started) return fail(GBPT_ERR_STATE, "renderer has not rendered yet");
+  CkHeader h{};
+  std::memcpy(h.magic, "GBPTCKP1", 8);
+  h.version = 1;
+  h.W = r->W;
+  h.H = r->H;
+  h.mode = r->mode;
+  h.frame = r->frame;
+  h.started = r->started ? 1u : 0u;
+  h.bilatIs2 = r->bilatOut == r->filtered2 ? 1u : 0u;
+  h.triN = r->lastTriN;
+  h.nodeN = r->lastNodeN;
+  std::memcpy(h.camBasis, r->camBasis, sizeof(h.camBasis));
+  h.debugMode = r->debugMode;
+  h.p = r->p;
+  char* out = static_cast<char*>(buf);
+  std::memcpy(out, &h, sizeof(h));
+  size_t at = sizeof(h);
+  for (const CkPlane& c : ck_planes(r)) {
+    CK(cudaMemcpyAsync(out + at, c.dev, c.bytes, cudaMemcpyDeviceToHost, r->st));
+    at += c.bytes;
+  }
+  CK(cudaStreamSynchronize(r->st));
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_renderer_restore(gbpt_renderer* r, const void* buf, size_t bytes) {
+  if (!r || !buf) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  if (bytes < sizeof(CkHeader)) return fail(GBPT_ERR_INVALID_ARG, "checkpoint truncated");
+  CkHeader h;
+  std::memcpy(&h, buf, sizeof(h));
+  if (std::memcmp(h.magic, "GBPTCKP1", 8) != 0 || h.version != 1)
+    return fail(GBPT_ERR_INVALID_ARG, "not a gbpt checkpoint");
+  if (h.W != r->W || h.H != r->H) return fail(GBPT_ERR_INVALID_ARG, "checkpoint image size differs");
+  if (bytes < ck_bytes(r)) return fail(GBPT_ERR_INVALID_ARG, "checkpoint truncated");
+  gbpt_status st = gbpt_set_params(r, &h.p);
+  if (st == GBPT_OK) st = gbpt_set_mode(r, h.mode);
+  if (st != GBPT_OK) return st;
+  st = ensure_alloc(r);
+  if (st != GBPT_OK) return st;
+  if (r->stLight) CK(cudaStreamSynchronize(r->stLight));  // no light pass still writes a cache
+  const char* in = static_cast<const char*>(buf);
+  size_t at = sizeof(h);
+  for (const CkPlane& c : ck_planes(r)) {
+    CK(cudaMemcpyAsync(c.dev, in + at, c.bytes, cudaMemcpyHostToDevice, r->st));
+    at += c.bytes;
+  }
+  CK(cudaStreamSynchronize(r->st));
+  r->frame = h.frame;
+  r->started = h.started != 0;
+  std::memcpy(r->camBasis, h.camBasis, sizeof(h.camBasis));
+  r->debugMode = h.debugMode;
+  r->bilatOut = h.bilatIs2 ? r->filtered2 : r->ab.filtered;
+  r->lastTraced = true;
+  r->epoch++;  // the light caches are made again
+  r->lightPending[0] = r->lightPending[1] = false;
+  r->resumeScene = true;
+  r->resumeTriN = h.triN;
+  r->resumeNodeN = h.nodeN;
   return GBPT_OK;
 }
 

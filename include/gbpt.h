@@ -221,6 +221,16 @@ gbpt_status gbpt_host_unregister(void* p);
 gbpt_status gbpt_read_buffer(gbpt_renderer* r, int32_t which, void* dst, size_t bytes, int32_t dst_is_device);
 /* Restart progressive accumulation (next frame is frame 0). */
 gbpt_status gbpt_reset(gbpt_renderer* r);
+/* Checkpoint / resume (the reference keeps only .NPRTENV presets with an
+ * optional converged image, src/cudapt.cpp:735-836).  A checkpoint holds the
+ * frame counter, camera, mode, parameters and every per-pixel accumulator; a
+ * renderer of the same size restored from it and given the same scene (same
+ * triangle and node counts) and camera continues the interrupted sequence to
+ * the bit.  gbpt_renderer_checkpoint_size gives the bytes the host buffer
+ * needs (about 150 per pixel). */
+gbpt_status gbpt_renderer_checkpoint_size(gbpt_renderer* r, size_t* bytes);
+gbpt_status gbpt_renderer_checkpoint(gbpt_renderer* r, void* buf, size_t bytes);
+gbpt_status gbpt_renderer_restore(gbpt_renderer* r, const void* buf, size_t bytes);
 /* CleanMem (src/cudaRTBDPTStream.cu:780-789): release device buffers now;
  * they are re-created on the next render. */
 gbpt_status gbpt_clean(gbpt_renderer* r);

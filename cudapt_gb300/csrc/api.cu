@@ -6,6 +6,7 @@
 // Unlike the reference there is no process-global device state: every scene
 // and renderer owns its buffers, and a renderer owns its CUDA stream.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <chrono>
@@ -758,7 +759,10 @@ gbpt_status render_impl(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam,
   const uint64_t launches0 = launch_count();
   r->evs.clear();
   for (uint32_t f = 0; f < frames; f++) {
+    // NVTX range per frame (free without a profiler attached; ncu --nvtx can filter on it)
+    nvtxRangePushA("gbpt frame");
     stt = frame_once(r, s, cam, timing);
+    nvtxRangePop();
     if (stt != GBPT_OK) return stt;
   }
   const size_t np = (size_t)r->W * r->H;

@@ -28,6 +28,7 @@
 // on whole requests (device time per camera path) until it has kTrials
 // samples, after which the class uses the fastest.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <chrono>
@@ -319,7 +320,9 @@ void gbpt_server::worker_main() {
     }
     req->tStart = Clock::now();
     std::string err;
+    nvtxRangePushA("gbpt request");
     const gbpt_status st = run_request(this, pool, *req, err);
+    nvtxRangePop();
     {
       std::lock_guard<std::mutex> lock(mu);
       req->tEnd = Clock::now();

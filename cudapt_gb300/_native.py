@@ -120,6 +120,8 @@ SIGNATURES = {
     "gbpt_server_create": (i32, [u32, ctypes.c_uint64, vp]),
     "gbpt_server_destroy": (i32, [vp]),
     "gbpt_server_set_policy": (i32, [vp, i32]),
+    "gbpt_selftest_wait_timeout": (i32, [vp]),
+    "gbpt_test_fail_allocations": (i32, [ctypes.c_int64]),
     "gbpt_renderer_checkpoint_size": (i32, [vp, vp]),
     "gbpt_renderer_checkpoint": (i32, [vp, vp, ctypes.c_size_t]),
     "gbpt_renderer_restore": (i32, [vp, vp, ctypes.c_size_t]),

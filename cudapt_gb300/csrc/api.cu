@@ -9,6 +9,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -42,10 +43,19 @@ gbpt_status fail(gbpt_status st, const std::string& s) {
 
 namespace {
 
+// host-side fault injection for tests (gbpt_test_fail_allocations): when
+// >= 0, the device allocations of this file fail once this many more have
+// succeeded
+std::atomic<int64_t> g_failAfter{-1};
+
 template <typename T>
 cudaError_t dalloc(T** p, size_t n) {
   *p = nullptr;
   if (n == 0) n = 1;
+  if (g_failAfter.load(std::memory_order_relaxed) >= 0 && g_failAfter.fetch_sub(1) <= 0) {
+    g_failAfter.store(0);
+    return cudaErrorMemoryAllocation;
+  }
   return cudaMalloc((void**)p, n * sizeof(T));
 }
 template <typename T>
@@ -1415,6 +1425,41 @@ gbpt_status gbpt_renderer_restore(gbpt_renderer* r, const void* buf, size_t byte
   r->resumeScene = true;
   r->resumeTriN = h.triN;
   r->resumeNodeN = h.nodeN;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_test_fail_allocations(int64_t after) {
+  g_failAfter.store(after < 0 ? -1 : after);
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_selftest_wait_timeout(double* elapsed_ms) {
+  uint32_t* coop = nullptr;
+  DevCounters* ctr = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  gbpt_status st = GBPT_OK;
+  uint32_t flags = 0;
+  float ms = 0.f;
+  cudaError_t e = dalloc(&coop, 4);
+  if (!e) e = dalloc(&ctr, 1);
+  if (!e) e = cudaMemset(coop, 0, 16);
+  if (!e) e = cudaMemset(ctr, 0, sizeof(DevCounters));
+  if (!e) e = cudaEventCreate(&e0);
+  if (!e) e = cudaEventCreate(&e1);
+  if (!e) e = cudaEventRecord(e0, nullptr);
+  if (!e) e = launch_barrier_selftest(coop, ctr, 2, nullptr);
+  if (!e) e = cudaEventRecord(e1, nullptr);
+  if (!e) e = cudaEventSynchronize(e1);
+  if (!e) e = cudaEventElapsedTime(&ms, e0, e1);
+  if (!e) e = cudaMemcpy(&flags, &ctr->errFlags, 4, cudaMemcpyDeviceToHost);
+  if (e) st = fail(GBPT_ERR_CUDA, std::string("wait self-test: ") + cudaGetErrorString(e));
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  dfree(coop);
+  dfree(ctr);
+  if (st != GBPT_OK) return st;
+  if (elapsed_ms) *elapsed_ms = ms;
+  if (flags & 4u) return fail(GBPT_ERR_TIMEOUT, "grid barrier wait ran out (self-test)");
   return GBPT_OK;
 }
 

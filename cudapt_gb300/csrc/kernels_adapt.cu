@@ -568,6 +568,13 @@ __device__ __forceinline__ bool grid_barrier(uint32_t* coop, uint32_t nblocks, D
   return ok != 0u;
 }
 
+// Failure-detection self-test: a grid barrier that waits for one block more
+// than are launched, so nobody releases it and every block's bounded wait
+// runs out (errFlags bit 2, as in the binary allocator).
+__global__ void k_barrier_selftest(uint32_t* coop, uint32_t nblocks, DevCounters* ctr) {
+  grid_barrier(coop, nblocks + 1u, ctr);
+}
+
 __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* ws) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   __syncthreads();
@@ -962,6 +969,12 @@ cudaError_t launch_adapt_accum(const FrameArgs& a, const RenderBuffers& b, const
     k_accum_huge<false><<<gh, kHugeThreads, 0, st>>>(a, b, ab, result, sampleN, gpos, gnorm, gdiff);
   }
   note_launches(4);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_barrier_selftest(uint32_t* coop, DevCounters* ctr, uint32_t blocks, cudaStream_t st) {
+  k_barrier_selftest<<<blocks, 32, 0, st>>>(coop, blocks, ctr);
+  note_launches(1);
   return cudaGetLastError();
 }
 

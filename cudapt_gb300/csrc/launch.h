@@ -125,6 +125,8 @@ uint32_t walk_refill_for(uint32_t requested);
 // Queries (once) the launch shapes of the wavefront kernels, which also loads
 // them: call before the first stream capture.
 void prepare_launches();
+// `blocks` CTAs wait at a grid barrier sized for blocks + 1 (failure-detection self-test)
+cudaError_t launch_barrier_selftest(uint32_t* coop, DevCounters* ctr, uint32_t blocks, cudaStream_t st);
 cudaError_t launch_apply(const FrameArgs& a, const RenderBuffers& b, float* result, uint32_t* sampleN, float* gpos,
                          float* gnorm, float* gdiff, cudaStream_t st);
 // filter-only mode (src/cudaRTBDPTStreamBilat.cu:989-1051): running means of

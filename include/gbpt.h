@@ -399,6 +399,19 @@ gbpt_status gbpt_server_release(gbpt_server* s, uint64_t id);
 gbpt_status gbpt_server_tuned(gbpt_server* s, int32_t mode, uint32_t depth, uint32_t width, uint32_t height,
                               uint32_t* walk_refill, int32_t* tail_from, uint32_t* samples);
 
+/* ---- failure detection ------------------------------------------------------
+ * Device waits (the binary allocator's grid barrier, the learned allocator's
+ * tensor-core completions) are bounded: one that runs out sets a bit of the
+ * renderer's device error word and its kernel returns, and the next host call
+ * reports GBPT_ERR_TIMEOUT with the context still usable.  This self-test
+ * runs the grid barrier with one block missing, so its wait runs out (about
+ * a second); it returns GBPT_ERR_TIMEOUT, and *elapsed_ms the wait's length. */
+gbpt_status gbpt_selftest_wait_timeout(double* elapsed_ms);
+/* Host-side fault injection for tests: after `after` more successful device
+ * allocations of the renderer / scene code, the following ones fail (as an
+ * out-of-memory device would) until called again with after < 0. */
+gbpt_status gbpt_test_fail_allocations(int64_t after);
+
 /* ---- device math, exposed for verification -------------------------------
  * Evaluated by a kernel on host arrays x/out (copied in and out).
  * which: 0 sin, 1 cos, 2 exp, 3 round-down sqrt, 4 x^5. */

@@ -301,7 +301,9 @@ def bench_gpu(args):
                      "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4) if achieved else None, "peak_kind": peak_kind,
                      "traffic": traffic,
-                     "algorithmic_bytes_per_frame": int(trace_bytes)},
+                     "algorithmic_bytes_per_frame": int(trace_bytes),
+                     # the tree and triangles are L2-resident: the L2 side of the same walks
+                     "l2": l2_side(args.workload, trace_ms)},
         "filter_roofline": filter_roofline(phases, args.steps, np_, peak) if WL[3] == 1 else None,
         "wide_traversal": wide,
         "learned_sampler": learned_sampler_summary(),
@@ -337,6 +339,19 @@ def serving_run(gb, n=64, rate=200.0, seed=0, workers=4):
     return summary
 
 
+def l2_side(workload, trace_ms):
+    """L2 bytes of one frame's walks (32-byte sectors, profiles/walk_traffic_<workload>.txt)
+    over this run's walk time, with the walk kernel's L2 throughput in percent of
+    peak as ncu reports it (profiles/k_walk_k_tail_interior_1024x768.md)."""
+    b = profiled_traffic(workload, "l2_bytes_per_frame")
+    if b is None or not trace_ms:
+        return None
+    return {"bytes_per_frame": b, "achieved_GBs": round(b / (trace_ms / 1e3) / 1e9, 1),
+            "throughput_pct_of_peak_ncu": [19.7, 15.1],
+            "note": "L2 serves the walks' node and triangle fetches that miss L1 (79-80% L1 hit rate); "
+                    "L2 throughput 15-20% of peak: latency-bound, not bandwidth-bound"}
+
+
 def filter_roofline(phases, steps, np_, peak):
     """Bilateral filter of a budgeted frame against its compulsory traffic: the colour,
     position and normal planes read (12 B per pixel each) and 12 B per pixel written."""
@@ -370,17 +385,18 @@ def learned_sampler_summary():
     return out
 
 
-def profiled_traffic(workload):
-    """DRAM bytes (read + write) of the BVH-walk launches of one frame, from the
-    committed ncu summary of this workload (profiles/walk_traffic_<workload>.txt,
-    line ``traffic_bytes_per_frame <n>``); None when no capture exists."""
+def profiled_traffic(workload, key="traffic_bytes_per_frame"):
+    """A figure of the BVH-walk launches of one frame from the committed ncu
+    summary of this workload (profiles/walk_traffic_<workload>.txt, line
+    ``<key> <n>``): DRAM bytes (read + write) by default, ``l2_bytes_per_frame``
+    for the L2's; None when no capture exists."""
     p = os.path.join(ROOT, "profiles", f"walk_traffic_{workload}.txt")
     if not os.path.exists(p):
         return None
     with open(p) as f:
         for ln in f:
             parts = ln.split()
-            if len(parts) == 2 and parts[0] == "traffic_bytes_per_frame":
+            if len(parts) == 2 and parts[0] == key:
                 return int(parts[1])
     return None
 

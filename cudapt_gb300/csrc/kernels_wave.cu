@@ -416,7 +416,17 @@ __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, Rend
         }
       }
     }
-    if (has && (any ? w.step<kCount>(S, stack, true, nnS, ntS) : w.step<kCount>(S, stack, false, nnE, ntE))) {
+    // one inlined walk step for both ray kinds (a runtime any-hit flag), so a
+    // warp holding extension and shadow rays does not run two copies of it;
+    // the counting variant keeps separate counters per kind
+    bool fin = false;
+    if (has) {
+      if (kCount)
+        fin = any ? w.template step<kCount>(S, stack, true, nnS, ntS) : w.template step<kCount>(S, stack, false, nnE, ntE);
+      else
+        fin = w.template step<kCount>(S, stack, any, nnE, ntE);
+    }
+    if (fin) {
       has = false;
       if (any) {
         if (!w.hit()) {  // unoccluded: the connection counts (:716-721)
@@ -672,7 +682,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_tail(DevScene S, FrameArgs a, Ren
     }
     if (mode == kIdle) continue;
     const bool anyHit = mode == kPathShadow;
-    const bool done = anyHit ? w.step<kCount>(S, stack, true, nnS, ntS) : w.step<kCount>(S, stack, false, nnE, ntE);
+    const bool done = kCount ? (anyHit ? w.template step<kCount>(S, stack, true, nnS, ntS)
+                                       : w.template step<kCount>(S, stack, false, nnE, ntE))
+                             : w.template step<kCount>(S, stack, anyHit, nnE, ntE);
     if (!done) continue;
     if (anyHit) {
       shRays++;

@@ -878,12 +878,15 @@ __global__ void k_trace_rays(DevScene S, const float* rays, uint32_t n, float ma
 int g_sm = 0;
 
 // Idle lanes of a warp that trigger a refill in k_walk / k_tail (tuning
-// knob, GBPT_WALK_REFILL, 1..32; 20 by default: measured 16-20 best on the
-// interior, 28-32 lose 2-7%).
-uint32_t walk_refill() {
+// knob, GBPT_WALK_REFILL, 1..32; 0 when unset).  Defaults, measured on the
+// interior, hall and Cornell workloads: 8 for the reference order (4-10
+// within 1%, 20 3-4% slower), 20 for the wide order (10-20 within 1%, 4 2-3%
+// slower).
+uint32_t walk_refill_env() {
   static uint32_t v = [] {
     const char* e = std::getenv("GBPT_WALK_REFILL");
-    int x = e ? std::atoi(e) : 20;
+    if (!e) return 0u;
+    int x = std::atoi(e);
     return (uint32_t)(x < 1 ? 1 : x > 32 ? 32 : x);
   }();
   return v;
@@ -956,14 +959,14 @@ template <bool kCount, bool kWide>
 void tail_variant(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn, uint32_t depth0,
                   cudaStream_t st) {
   const uint32_t g = tail_grid<kCount, kWide>();
-  k_tail<kCount, kWide><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill_for(a.refill));
+  k_tail<kCount, kWide><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill_for(a.refill, kWide));
 }
 
 cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
                         int shReset, bool shDirect, cudaStream_t st) {
   const uint32_t sd = (a.bilat && shDirect) ? 1u : 0u;
   const bool wide = S.traversal == 1 && S.wide;
-  const uint32_t rf = walk_refill_for(a.refill);
+  const uint32_t rf = walk_refill_for(a.refill, wide);
   if (a.counting) {
     if (wide) walk_variant<true, true>(S, b, in, shIn, shReset, sd, rf, st);
     else walk_variant<true, false>(S, b, in, shIn, shReset, sd, rf, st);
@@ -1017,8 +1020,10 @@ uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested) {
   return v < 0 ? eyeDepth : (uint32_t)v;
 }
 
-uint32_t walk_refill_for(uint32_t requested) {
-  return (requested >= 1 && requested <= 32) ? requested : walk_refill();
+uint32_t walk_refill_for(uint32_t requested, bool wide) {
+  if (requested >= 1 && requested <= 32) return requested;
+  if (walk_refill_env()) return walk_refill_env();
+  return wide ? 20u : 8u;
 }
 
 cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t depth,

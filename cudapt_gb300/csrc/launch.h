@@ -120,8 +120,8 @@ cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffe
 // none in the wide order
 uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested);
 // refill threshold of the persistent walks: `requested` when 1..32, else
-// GBPT_WALK_REFILL when set, else 20
-uint32_t walk_refill_for(uint32_t requested);
+// GBPT_WALK_REFILL when set, else 8 (reference order) or 20 (wide order)
+uint32_t walk_refill_for(uint32_t requested, bool wide);
 // Queries (once) the launch shapes of the wavefront kernels, which also loads
 // them: call before the first stream capture.
 void prepare_launches();

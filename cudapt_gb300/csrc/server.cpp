@@ -71,10 +71,10 @@ struct Knobs {
 // percent on the large workloads (small images favour earlier refills and
 // earlier tails, whose per-bounce launches wait on their slowest ray).
 std::vector<Knobs> candidates(uint32_t depth) {
-  std::vector<Knobs> c = {{20, -1}, {12, -1}, {28, -1}};
-  if (depth > 3) c.push_back({20, (int32_t)depth - 3});
-  if (depth > 5) c.push_back({20, (int32_t)depth - 5});
-  c.push_back({20, (int32_t)depth});  // no tail kernel
+  std::vector<Knobs> c = {{8, -1}, {4, -1}, {16, -1}};
+  if (depth > 3) c.push_back({8, (int32_t)depth - 3});
+  if (depth > 5) c.push_back({8, (int32_t)depth - 5});
+  c.push_back({8, (int32_t)depth});  // no tail kernel
   return c;
 }
 
@@ -443,7 +443,7 @@ gbpt_status gbpt_server_tuned(gbpt_server* s, int32_t mode, uint32_t depth, uint
   std::lock_guard<std::mutex> lock(s->mu);
   auto it = s->tuning.find(ClassKey{mode, depth, probe.size()});
   if (it == s->tuning.end()) {
-    *walk_refill = 20;
+    *walk_refill = 8;
     *tail_from = -1;
     *samples = 0;
     return GBPT_OK;

@@ -94,7 +94,8 @@ typedef struct gbpt_params {
   uint32_t render_iterations; /* "Render Iteration" (5): frames that trace paths; 0 = no limit */
   uint32_t pt_depth_max;    /* "PTSC" bounce cap, NORMALRAY_BOUND_MAX of src/cudaRTPTStream.cu:6 (10) */
   /* scheduling of the wavefront (results do not depend on either) */
-  uint32_t walk_refill;     /* idle lanes of a warp that make a persistent walk fetch new rays (1..32; 0: 20) */
+  uint32_t walk_refill;     /* idle lanes of a warp that make a persistent walk fetch new rays
+                               (1..32; 0: 8 in the reference order, 20 in the wide order) */
   int32_t tail_from;        /* first bounce the per-path tail kernel carries (>= the depth cap: none;
                                -1: depth - 4 when the cap exceeds 6 in the reference order, none in the wide order) */
 } gbpt_params;

@@ -372,6 +372,13 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, uint32_t v
 // 5 resident CTAs per SM (48 registers) for the reference order: measured
 // 1-2% faster than 4 or 6 on the interior and hall workloads; 4 for the wide
 // walk (its wide-node step needs more registers).
+// walk steps per refill check: 2 in the wide order (+1-2%), 1 in the
+// reference order (2 measured 3-5% slower there)
+template <bool kWide>
+__host__ __device__ constexpr int walk_steps() {
+  return kWide ? 2 : 1;
+}
+
 template <bool kCount, bool kWide>
 __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, RenderBuffers b, int in, int shIn,
                                                               int shReset, uint32_t shDirect, uint32_t kRefill) {
@@ -416,30 +423,35 @@ __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, Rend
         }
       }
     }
-    // one inlined walk step for both ray kinds (a runtime any-hit flag), so a
-    // warp holding extension and shadow rays does not run two copies of it;
-    // the counting variant keeps separate counters per kind
-    bool fin = false;
-    if (has) {
-      if (kCount)
-        fin = any ? w.template step<kCount>(S, stack, true, nnS, ntS) : w.template step<kCount>(S, stack, false, nnE, ntE);
-      else
-        fin = w.template step<kCount>(S, stack, any, nnE, ntE);
-    }
-    if (fin) {
-      has = false;
-      if (any) {
-        if (!w.hit()) {  // unoccluded: the connection counts (:716-721)
-          const float4 A = sh[3 * (size_t)item], C = sh[3 * (size_t)item + 2];
-          const uint32_t slot = __float_as_uint(A.w);
-          const float4 r = b.res[slot];
-          b.res[slot] =
-              make_float4(r.x + C.x, r.y + C.y, r.z + C.z, __uint_as_float(__float_as_uint(r.w) + 4u));
-          if (shDirect) direct_connect(b.dsm, slot, C);
+    // walk_steps() steps per refill check: the ballot and refill test are paid
+    // once for them (a lane whose walk ends in the first waits out the rest)
+#pragma unroll 1
+    for (int u = 0; u < walk_steps<kWide>(); u++) {
+      // one inlined walk step for both ray kinds (a runtime any-hit flag), so a
+      // warp holding extension and shadow rays does not run two copies of it;
+      // the counting variant keeps separate counters per kind
+      bool fin = false;
+      if (has) {
+        if (kCount)
+          fin = any ? w.template step<kCount>(S, stack, true, nnS, ntS) : w.template step<kCount>(S, stack, false, nnE, ntE);
+        else
+          fin = w.template step<kCount>(S, stack, any, nnE, ntE);
+      }
+      if (fin) {
+        has = false;
+        if (any) {
+          if (!w.hit()) {  // unoccluded: the connection counts (:716-721)
+            const float4 A = sh[3 * (size_t)item], C = sh[3 * (size_t)item + 2];
+            const uint32_t slot = __float_as_uint(A.w);
+            const float4 r = b.res[slot];
+            b.res[slot] =
+                make_float4(r.x + C.x, r.y + C.y, r.z + C.z, __uint_as_float(__float_as_uint(r.w) + 4u));
+            if (shDirect) direct_connect(b.dsm, slot, C);
+          }
+        } else {
+          b.hit[item] = w.hit() ? make_float4(w.minT, __uint_as_float(w.best), w.bu, w.bv)
+                                : make_float4(-1.f, 0.f, 0.f, 0.f);
         }
-      } else {
-        b.hit[item] = w.hit() ? make_float4(w.minT, __uint_as_float(w.best), w.bu, w.bv)
-                              : make_float4(-1.f, 0.f, 0.f, 0.f);
       }
     }
   }

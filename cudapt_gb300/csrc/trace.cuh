@@ -155,7 +155,9 @@ struct Walk {
   }
 
   // One pop of TracePrimitive's loop.  Returns true when the walk is over:
-  // stack empty, 2048 pops done, or (anyHit) a hit closer than maxDist found.
+  // (anyHit) a hit closer than maxDist found, or -- at the start of the call
+  // after the last pop -- stack empty or 2048 pops done (testing that once per
+  // call instead of after every pop costs one more call per ray).
   template <bool kCount>
   __device__ __forceinline__ bool step(const DevScene& S, uint32_t* stack, bool anyHit, uint32_t& nNodes,
                                        uint32_t& nTris) {
@@ -177,7 +179,7 @@ struct Walk {
     const float maxmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
     float tb = kInf;
     if (minmax >= maxmin && (minmax > 0.f || maxmin > 0.f)) tb = (maxmin > kGtEps9) ? maxmin : 0.f;
-    if (!(tb >= 0.f && tb < minT)) return sp < 0 || steps >= 2048u;
+    if (!(tb >= 0.f && tb < minT)) return false;
     const uint32_t off = __float_as_uint(a.w);
     const uint32_t tn = __float_as_uint(b.w);
     if (tn == 0) {
@@ -187,7 +189,7 @@ struct Walk {
         sp += 2;
         tos = cur + off;
       }
-      return sp < 0 || steps >= 2048u;
+      return false;
     }
     for (uint32_t i = off; i < off + tn; i++) {
       float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), e0 = p0, e1 = p0;
@@ -219,7 +221,7 @@ struct Walk {
         if (anyHit) return true;
       }
     }
-    return sp < 0 || steps >= 2048u;
+    return false;
   }
 
   __device__ __forceinline__ bool hit() const { return minT < maxDist; }

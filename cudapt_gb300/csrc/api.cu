@@ -142,7 +142,10 @@ gbpt_status upload_wide(gbpt_scene* s) {
 gbpt_status upload_scene(gbpt_scene* s) {
   s->free_dev();
   const uint32_t nt = (uint32_t)s->trisOrdered.size(), nn = s->bvh.nodeN;
-  std::vector<float4> nodes((size_t)nn * 2), tris((size_t)nt * 3), shade((size_t)nt * 5);
+  // one all-zero node record and one all-zero triangle record after the
+  // arrays: a walk reads them for ids past the end (the reference's texture
+  // fetches return zeros there) without a bounds-checked load
+  std::vector<float4> nodes((size_t)(nn + 1) * 2), tris((size_t)(nt + 1) * 3), shade((size_t)nt * 5);
   for (uint32_t i = 0; i < nn; i++) {
     const float* b = &s->bvh.bounds[(size_t)i * 6];
     nodes[2 * i] = make_float4(b[0], b[1], b[2], as_f(s->bvh.offOrTSTN[2 * i]));

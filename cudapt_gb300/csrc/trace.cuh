@@ -14,7 +14,8 @@
 // are hoisted out of the loop; they are the same values every iteration.
 // A node is fetched with one 32-byte non-coherent load (ld.global.nc.v8, one
 // sector; sm_100 and later), a triangle with three 16-byte __ldg loads; an
-// out-of-range id reads zeros like the reference's texture fetch.
+// out-of-range id reads zeros like the reference's texture fetch: ids are
+// clamped to one all-zero record stored after each array.
 #pragma once
 #include "gbpt_math.cuh"
 #include "launch.h"
@@ -52,10 +53,8 @@ __device__ __forceinline__ bool trace_ref(const DevScene& S, gb::f3 o, gb::f3 d,
   const float4* __restrict__ tris = S.tris;
   while (sp >= 0 && steps++ < 2048u) {
     const uint32_t cur = stack[sp--];
-    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-    if (cur < S.nodeN) {
-      ldg_node(nodes + 2 * (size_t)cur, a, b);
-    }
+    float4 a, b;  // an id past the tree reads the zero record after it
+    ldg_node(nodes + 2 * (size_t)min(cur, S.nodeN), a, b);
     if (kCount) nNodes++;
     const float t0x = (a.x - o.x) * inv.x, t1x = (b.x - o.x) * inv.x;
     const float t0y = (a.y - o.y) * inv.y, t1y = (b.y - o.y) * inv.y;
@@ -75,12 +74,8 @@ __device__ __forceinline__ bool trace_ref(const DevScene& S, gb::f3 o, gb::f3 d,
       continue;
     }
     for (uint32_t i = off; i < off + tn; i++) {
-      float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), e0 = p0, e1 = p0;
-      if (i < S.triN) {
-        p0 = __ldg(tris + 3 * (size_t)i);
-        e0 = __ldg(tris + 3 * (size_t)i + 1);
-        e1 = __ldg(tris + 3 * (size_t)i + 2);
-      }
+      const size_t ti = 3 * (size_t)min(i, S.triN);  // past the end: the zero record
+      const float4 p0 = __ldg(tris + ti), e0 = __ldg(tris + ti + 1), e1 = __ldg(tris + ti + 2);
       if (kCount) nTris++;
       const f3 E0 = mk(e0.x, e0.y, e0.z), E1 = mk(e1.x, e1.y, e1.z);
       if (cullback && dot(cross(E0, E1), d) > 0.f) continue;
@@ -167,10 +162,8 @@ struct Walk {
     const uint32_t cur = tos;
     sp--;
     if (sp >= 0) tos = stack[sp];
-    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-    if (cur < S.nodeN) {
-      ldg_node(S.nodes + 2 * (size_t)cur, a, b);
-    }
+    float4 a, b;  // an id past the tree reads the zero record after it
+    ldg_node(S.nodes + 2 * (size_t)min(cur, S.nodeN), a, b);
     if (kCount) nNodes++;
     const float t0x = (a.x - o.x) * inv.x, t1x = (b.x - o.x) * inv.x;
     const float t0y = (a.y - o.y) * inv.y, t1y = (b.y - o.y) * inv.y;
@@ -192,12 +185,8 @@ struct Walk {
       return false;
     }
     for (uint32_t i = off; i < off + tn; i++) {
-      float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), e0 = p0, e1 = p0;
-      if (i < S.triN) {
-        p0 = __ldg(S.tris + 3 * (size_t)i);
-        e0 = __ldg(S.tris + 3 * (size_t)i + 1);
-        e1 = __ldg(S.tris + 3 * (size_t)i + 2);
-      }
+      const size_t ti = 3 * (size_t)min(i, S.triN);  // past the end: the zero record
+      const float4 p0 = __ldg(S.tris + ti), e0 = __ldg(S.tris + ti + 1), e1 = __ldg(S.tris + ti + 2);
       if (kCount) nTris++;
       const f3 E0 = mk(e0.x, e0.y, e0.z), E1 = mk(e1.x, e1.y, e1.z);
       const f3 de2 = cross(d, E1);
@@ -299,12 +288,8 @@ struct Walk4 {
         cnt = __float_as_uint(__ldg(S.nodes + 2 * (size_t)nid + 1).w);
       }
       for (uint32_t i = first; i < first + cnt; i++) {
-        float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), e0 = p0, e1 = p0;
-        if (i < S.triN) {
-          p0 = __ldg(S.tris + 3 * (size_t)i);
-          e0 = __ldg(S.tris + 3 * (size_t)i + 1);
-          e1 = __ldg(S.tris + 3 * (size_t)i + 2);
-        }
+        const size_t ti = 3 * (size_t)min(i, S.triN);  // past the end: the zero record
+        const float4 p0 = __ldg(S.tris + ti), e0 = __ldg(S.tris + ti + 1), e1 = __ldg(S.tris + ti + 2);
         if (kCount) nTris++;
         const f3 E0 = mk(e0.x, e0.y, e0.z), E1 = mk(e1.x, e1.y, e1.z);
         const f3 de2 = cross(d, E1);

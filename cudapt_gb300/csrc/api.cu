@@ -145,7 +145,7 @@ gbpt_status upload_scene(gbpt_scene* s) {
   // one all-zero node record and one all-zero triangle record after the
   // arrays: a walk reads them for ids past the end (the reference's texture
   // fetches return zeros there) without a bounds-checked load
-  std::vector<float4> nodes((size_t)(nn + 1) * 2), tris((size_t)(nt + 1) * 3), shade((size_t)nt * 5);
+  std::vector<float4> nodes((size_t)(nn + 1) * 2), tris((size_t)(nt + 1) * 4), shade((size_t)nt * 5);
   for (uint32_t i = 0; i < nn; i++) {
     const float* b = &s->bvh.bounds[(size_t)i * 6];
     nodes[2 * i] = make_float4(b[0], b[1], b[2], as_f(s->bvh.offOrTSTN[2 * i]));
@@ -155,9 +155,9 @@ gbpt_status upload_scene(gbpt_scene* s) {
     const gbpt_triangle& t = s->trisOrdered[i];
     const gbpt_vertex &a = s->verts[t.v0], &b = s->verts[t.v1], &c = s->verts[t.v2];
     // src/cudaRTCommon.cu:507-509: p0, p1 - p0, p2 - p0 (host float subtraction)
-    tris[3 * i] = make_float4(a.pos[0], a.pos[1], a.pos[2], 0.f);
-    tris[3 * i + 1] = make_float4(b.pos[0] - a.pos[0], b.pos[1] - a.pos[1], b.pos[2] - a.pos[2], 0.f);
-    tris[3 * i + 2] = make_float4(c.pos[0] - a.pos[0], c.pos[1] - a.pos[1], c.pos[2] - a.pos[2], 0.f);
+    tris[4 * i] = make_float4(a.pos[0], a.pos[1], a.pos[2], 0.f);
+    tris[4 * i + 1] = make_float4(b.pos[0] - a.pos[0], b.pos[1] - a.pos[1], b.pos[2] - a.pos[2], 0.f);
+    tris[4 * i + 2] = make_float4(c.pos[0] - a.pos[0], c.pos[1] - a.pos[1], c.pos[2] - a.pos[2], 0.f);
     shade[5 * i] = make_float4(a.norm[0], a.norm[1], a.norm[2], a.pos[0]);
     shade[5 * i + 1] = make_float4(b.norm[0], b.norm[1], b.norm[2], a.pos[1]);
     shade[5 * i + 2] = make_float4(c.norm[0], c.norm[1], c.norm[2], a.pos[2]);

@@ -25,7 +25,7 @@ namespace gbpt {
 constexpr uint32_t kWideEmpty = 0xFFFFFFFFu, kWideLeaf = 0x80000000u, kWideTri = 0xC0000000u;
 struct DevScene {
   const float4* nodes = nullptr;  // nodeN + 1 records of 2 float4, the last all zeros
-  const float4* tris = nullptr;   // triN + 1 records of 3 float4, the last all zeros
+  const float4* tris = nullptr;   // triN + 1 records of 4 float4 (p0, p1 - p0, p2 - p0, 0), the last all zeros
   const float4* shade = nullptr;
   const float4* mats = nullptr;
   const uint32_t* lightTri = nullptr;

@@ -13,7 +13,8 @@
 // The per-ray constants of those two tests (1/escapeZero(dir), o + eps*dir)
 // are hoisted out of the loop; they are the same values every iteration.
 // A node is fetched with one 32-byte non-coherent load (ld.global.nc.v8, one
-// sector; sm_100 and later), a triangle with three 16-byte __ldg loads; an
+// sector; sm_100 and later), a triangle (64-byte record) with one 32-byte and
+// one 16-byte load; an
 // out-of-range id reads zeros like the reference's texture fetch: ids are
 // clamped to one all-zero record stored after each array.
 #pragma once
@@ -74,8 +75,10 @@ __device__ __forceinline__ bool trace_ref(const DevScene& S, gb::f3 o, gb::f3 d,
       continue;
     }
     for (uint32_t i = off; i < off + tn; i++) {
-      const size_t ti = 3 * (size_t)min(i, S.triN);  // past the end: the zero record
-      const float4 p0 = __ldg(tris + ti), e0 = __ldg(tris + ti + 1), e1 = __ldg(tris + ti + 2);
+      const size_t ti = 4 * (size_t)min(i, S.triN);  // past the end: the zero record
+      float4 p0, e0;
+      ldg_node(tris + ti, p0, e0);
+      const float4 e1 = __ldg(tris + ti + 2);
       if (kCount) nTris++;
       const f3 E0 = mk(e0.x, e0.y, e0.z), E1 = mk(e1.x, e1.y, e1.z);
       if (cullback && dot(cross(E0, E1), d) > 0.f) continue;
@@ -185,8 +188,10 @@ struct Walk {
       return false;
     }
     for (uint32_t i = off; i < off + tn; i++) {
-      const size_t ti = 3 * (size_t)min(i, S.triN);  // past the end: the zero record
-      const float4 p0 = __ldg(S.tris + ti), e0 = __ldg(S.tris + ti + 1), e1 = __ldg(S.tris + ti + 2);
+      const size_t ti = 4 * (size_t)min(i, S.triN);  // past the end: the zero record
+      float4 p0, e0;
+      ldg_node(S.tris + ti, p0, e0);
+      const float4 e1 = __ldg(S.tris + ti + 2);
       if (kCount) nTris++;
       const f3 E0 = mk(e0.x, e0.y, e0.z), E1 = mk(e1.x, e1.y, e1.z);
       const f3 de2 = cross(d, E1);
@@ -288,8 +293,10 @@ struct Walk4 {
         cnt = __float_as_uint(__ldg(S.nodes + 2 * (size_t)nid + 1).w);
       }
       for (uint32_t i = first; i < first + cnt; i++) {
-        const size_t ti = 3 * (size_t)min(i, S.triN);  // past the end: the zero record
-        const float4 p0 = __ldg(S.tris + ti), e0 = __ldg(S.tris + ti + 1), e1 = __ldg(S.tris + ti + 2);
+        const size_t ti = 4 * (size_t)min(i, S.triN);  // past the end: the zero record
+        float4 p0, e0;
+        ldg_node(S.tris + ti, p0, e0);
+        const float4 e1 = __ldg(S.tris + ti + 2);
         if (kCount) nTris++;
         const f3 E0 = mk(e0.x, e0.y, e0.z), E1 = mk(e1.x, e1.y, e1.z);
         const f3 de2 = cross(d, E1);

@@ -1597,7 +1597,7 @@ gbpt_status gbpt_bilateral(const float* color, const float* pos, const float* no
 }
 
 gbpt_status gbpt_fmath(int32_t which, const float* x, uint32_t n, float* out) {
-  if (!x || !out || which < 0 || which > 4) return fail(GBPT_ERR_INVALID_ARG, "bad argument");
+  if (!x || !out || which < 0 || which > 5) return fail(GBPT_ERR_INVALID_ARG, "bad argument");
   if (n == 0) return GBPT_OK;
   float *dx = nullptr, *dy = nullptr;
   CK(dalloc(&dx, n));

@@ -32,25 +32,62 @@ __device__ __forceinline__ float eucl(float ax, float ay, float az, float bx, fl
   return gb::exp_p(-mod / c2);
 }
 
+// gb::exp_p for arguments x <= 0 (or NaN), to the bit: the same reduction and
+// polynomial, with 2^k applied as one factor and the x < -87 case as a
+// select instead of a branch.  For -87 <= x <= 0, k = rint(x log2 e) lies in
+// [-126, 0], so 2^k is a normal number; exp_p's p * 2^k1 is then a normal
+// number (exact) and its second product p * 2^k1 * 2^k2 rounds exactly as
+// the single product p * 2^k does.
+__device__ __forceinline__ float exp_nonpos_p(float x) {
+  using namespace gb;
+  const float log2e = 0x1.715476p+0f;
+  const float ln2_hi = 0x1.62e430p-1f;
+  const float ln2_lo = -0x1.05c610p-29f;
+  const float kf = rint_(x * log2e);
+  float r = fma_(-kf, ln2_hi, x);
+  r = fma_(-kf, ln2_lo, r);
+  float p = fma_(r, 1.98412698e-04f, 1.38888889e-03f);
+  p = fma_(r, p, 8.33333333e-03f);
+  p = fma_(r, p, 4.16666667e-02f);
+  p = fma_(r, p, 1.66666667e-01f);
+  p = fma_(r, p, 0.5f);
+  p = fma_(r, p, 1.0f);
+  p = fma_(r, p, 1.0f);
+  const float res = p * bits_f((uint32_t)((int)kf + 127) << 23);
+  return (x < -87.0f) ? 0.0f : res;
+}
+
+// eucl() for the tile kernel: -mod / c2 <= 0 (or NaN) for c2 >= 0
+__device__ __forceinline__ float eucl_nonpos(float ax, float ay, float az, float bx, float by, float bz, float c2) {
+  float dx = bx - ax, dy = by - ay, dz = bz - az;
+  float mod = (dx * dx + dy * dy) + dz * dz;
+  return exp_nonpos_p(-mod / c2);
+}
+
 // Tap (x+j, y+i) with the reference's unsigned arithmetic: a coordinate left
 // of column 0 wraps to a huge value and min() sends it to the last column.
 __device__ __forceinline__ uint32_t wrapc(int g, uint32_t n) { return ((uint32_t)g < n) ? (uint32_t)g : n - 1; }
 
-// One 16x16 output tile; the (16+2r)^2 input window of every plane is
-// staged in shared memory (planes stored as float triples).
-template <bool kEmit>
+// One 16x16 output tile; the (16+2r)^2 input window is staged in shared
+// memory as one 48-byte record per texel -- colour, position, normal and (the
+// filter-only mode's fourth plane) emission packed into three float4 -- so a
+// tap is three 16-byte shared loads.  A quarter warp's eight consecutive
+// records start 12 words apart and cover all 32 banks once: no conflicts.
+// kR > 0 fixes the radius at compile time (the tap row is unrolled and its
+// weights live in registers); kR == 0 takes r at run time.
+template <bool kEmit, int kR>
 __global__ void __launch_bounds__(kTile* kTile) k_bilateral_tile(const float* __restrict__ color,
                                                                   const float* __restrict__ pos,
                                                                   const float* __restrict__ norm,
                                                                   const float* __restrict__ emit, uint32_t W,
                                                                   uint32_t H, float cc2, float pc2, float nc2,
-                                                                  float ec2, int r, const float* __restrict__ g,
+                                                                  float ec2, int rArg, const float* __restrict__ g,
                                                                   float* __restrict__ out) {
-  extern __shared__ float sm[];
+  extern __shared__ float4 smv[];
+  const int r = kR > 0 ? kR : rArg;
   const int T = kTile + 2 * r;
-  const int planes = kEmit ? 4 : 3;
-  float* sg = sm;                      // 2r+1 gaussian weights
-  float* tile = sm + ((2 * r + 1 + 3) & ~3);
+  float* sg = reinterpret_cast<float*>(smv);  // 2r+1 gaussian weights, padded to whole float4
+  float4* tile = smv + (2 * r + 1 + 3) / 4;
   const int x0 = blockIdx.x * kTile - r, y0 = blockIdx.y * kTile - r;
   const int tid = threadIdx.y * kTile + threadIdx.x;
   for (int k = tid; k < 2 * r + 1; k += kTile * kTile) sg[k] = g[k];
@@ -58,30 +95,46 @@ __global__ void __launch_bounds__(kTile* kTile) k_bilateral_tile(const float* __
     int ty = k / T, tx = k - ty * T;
     uint32_t gx = wrapc(x0 + tx, W), gy = wrapc(y0 + ty, H);
     size_t src = 3 * ((size_t)gy * W + gx);
-    float* dst = tile + 3 * (size_t)k * planes;
-    dst[0] = color[src]; dst[1] = color[src + 1]; dst[2] = color[src + 2];
-    dst[3] = pos[src];   dst[4] = pos[src + 1];   dst[5] = pos[src + 2];
-    dst[6] = norm[src];  dst[7] = norm[src + 1];  dst[8] = norm[src + 2];
-    if (kEmit) { dst[9] = emit[src]; dst[10] = emit[src + 1]; dst[11] = emit[src + 2]; }
+    float4* dst = tile + 3 * (size_t)k;
+    const float n2 = norm[src + 2];
+    dst[0] = make_float4(color[src], color[src + 1], color[src + 2], pos[src]);
+    dst[1] = make_float4(pos[src + 1], pos[src + 2], norm[src], norm[src + 1]);
+    dst[2] = kEmit ? make_float4(n2, emit[src], emit[src + 1], emit[src + 2]) : make_float4(n2, 0.f, 0.f, 0.f);
   }
   __syncthreads();
   const uint32_t x = blockIdx.x * kTile + threadIdx.x, y = blockIdx.y * kTile + threadIdx.y;
   if (x >= W || y >= H) return;
-  const float* cen = tile + 3 * (size_t)((threadIdx.y + r) * T + threadIdx.x + r) * planes;
+  const float4* c4 = tile + 3 * (size_t)((threadIdx.y + r) * T + threadIdx.x + r);
+  const float4 cA = c4[0], cB = c4[1], cC = c4[2];
   float sum = 0.f, tx = 0.f, ty = 0.f, tz = 0.f;
-  for (int i = -r; i <= r; i++) {
-    const float gi = sg[i + r];
-    for (int j = -r; j <= r; j++) {
-      const float* q = tile + 3 * (size_t)((threadIdx.y + r + i) * T + threadIdx.x + r + j) * planes;
-      float f = gi * sg[j + r];
-      f = f * eucl(q[0], q[1], q[2], cen[0], cen[1], cen[2], cc2);
-      f = f * eucl(q[3], q[4], q[5], cen[3], cen[4], cen[5], pc2);
-      f = f * eucl(q[6], q[7], q[8], cen[6], cen[7], cen[8], nc2);
-      if (kEmit) f = f * eucl(q[9], q[10], q[11], cen[9], cen[10], cen[11], ec2);
-      tx = tx + f * q[0];
-      ty = ty + f * q[1];
-      tz = tz + f * q[2];
-      sum = sum + f;
+  // one tap, in the reference's order of products and sums
+  auto tap = [&](const float4* q, float f) {
+    const float4 A = q[0], B = q[1], C = q[2];
+    f = f * eucl_nonpos(A.x, A.y, A.z, cA.x, cA.y, cA.z, cc2);
+    f = f * eucl_nonpos(A.w, B.x, B.y, cA.w, cB.x, cB.y, pc2);
+    f = f * eucl_nonpos(B.z, B.w, C.x, cB.z, cB.w, cC.x, nc2);
+    if (kEmit) f = f * eucl_nonpos(C.y, C.z, C.w, cC.y, cC.z, cC.w, ec2);
+    tx = tx + f * A.x;
+    ty = ty + f * A.y;
+    tz = tz + f * A.z;
+    sum = sum + f;
+  };
+  if constexpr (kR > 0) {
+    float gw[2 * kR + 1];
+#pragma unroll
+    for (int j = 0; j <= 2 * kR; j++) gw[j] = sg[j];
+#pragma unroll 1
+    for (int i = 0; i <= 2 * kR; i++) {
+      const float gi = sg[i];
+      const float4* row = tile + 3 * (size_t)((threadIdx.y + i) * T + threadIdx.x);
+#pragma unroll
+      for (int j = 0; j <= 2 * kR; j++) tap(row + 3 * j, gi * gw[j]);
+    }
+  } else {
+    for (int i = 0; i <= 2 * r; i++) {
+      const float gi = sg[i];
+      const float4* row = tile + 3 * (size_t)((threadIdx.y + i) * T + threadIdx.x);
+      for (int j = 0; j <= 2 * r; j++) tap(row + 3 * j, gi * sg[j]);
     }
   }
   float* o = out + 3 * ((size_t)y * W + x);
@@ -762,6 +815,7 @@ __global__ void k_fmath(int which, const float* x, uint32_t n, float* out) {
     case 2: r = gb::exp_p(v); break;
     case 3: r = gb::sqrt_rd_(v); break;
     case 4: r = gb::pow5(v); break;
+    case 5: r = exp_nonpos_p(v); break;
   }
   out[i] = r;
 }
@@ -788,16 +842,20 @@ cudaError_t launch_bilateral(const float* color, const float* pos, const float* 
   dim3 grid((W + kTile - 1) / kTile, (H + kTile - 1) / kTile), block(kTile, kTile);
   const int r = (int)radius;
   const int T = kTile + 2 * r;
-  const int planes = emit ? 4 : 3;
-  size_t smem = (size_t)(((2 * r + 1 + 3) & ~3) + 3 * T * T * planes) * sizeof(float);
+  const size_t smem = ((size_t)(2 * r + 1 + 3) / 4 + 3 * (size_t)T * T) * sizeof(float4);
   if (smem <= 200 * 1024) {
+    auto tile = [&](auto kern) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      kern<<<grid, block, smem, st>>>(color, pos, norm, emit, W, H, cc2, pc2, nc2, ec2, r, g, out);
+    };
     if (emit) {
-      cudaFuncSetAttribute(k_bilateral_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_bilateral_tile<true><<<grid, block, smem, st>>>(color, pos, norm, emit, W, H, cc2, pc2, nc2, ec2, r, g, out);
+      if (r == 4) tile(k_bilateral_tile<true, 4>);
+      else if (r == 5) tile(k_bilateral_tile<true, 5>);
+      else tile(k_bilateral_tile<true, 0>);
     } else {
-      cudaFuncSetAttribute(k_bilateral_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_bilateral_tile<false><<<grid, block, smem, st>>>(color, pos, norm, emit, W, H, cc2, pc2, nc2, ec2, r, g,
-                                                          out);
+      if (r == 4) tile(k_bilateral_tile<false, 4>);
+      else if (r == 5) tile(k_bilateral_tile<false, 5>);
+      else tile(k_bilateral_tile<false, 0>);
     }
   } else if (emit) {
     k_bilateral_direct<true><<<grid, block, 0, st>>>(color, pos, norm, emit, W, H, cc2, pc2, nc2, ec2, r, g, out);

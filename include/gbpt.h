@@ -415,7 +415,8 @@ gbpt_status gbpt_test_fail_allocations(int64_t after);
 
 /* ---- device math, exposed for verification -------------------------------
  * Evaluated by a kernel on host arrays x/out (copied in and out).
- * which: 0 sin, 1 cos, 2 exp, 3 round-down sqrt, 4 x^5. */
+ * which: 0 sin, 1 cos, 2 exp, 3 round-down sqrt, 4 x^5, 5 exp of an argument <= 0 as the
+ * bilateral filter's tile kernel evaluates it (equal to 2 there). */
 gbpt_status gbpt_fmath(int32_t which, const float* x, uint32_t n, float* out);
 /* Philox4x32-10 by a kernel: n counters (4 words each) -> 4 words each, host arrays. */
 gbpt_status gbpt_philox(const uint32_t* ctr, uint32_t n, uint32_t k0, uint32_t k1, uint32_t* out);

@@ -28,6 +28,24 @@ def test_fmath_bitexact(gbdev, orc):
         assert np.array_equal(out.view(np.uint32), want.view(np.uint32)), names[which]
 
 
+def test_exp_nonpositive_matches_exp(gbdev, orc):
+    """The bilateral tile kernel's exponential for arguments <= 0 equals exp_p to the bit: every 67th
+    float from -0 down to -90, every float within 2^-6 of the -87 cut and of the k = -126 turn, NaN."""
+    L = gbdev._native.load()
+    lo = np.float32(-90.0).view(np.uint32)
+    bits = np.arange(0x80000000, int(lo) + 1, 67, dtype=np.uint64).astype(np.uint32)
+    edges = [np.arange(int(np.float32(v - 2.0**-6).view(np.uint32)), int(np.float32(v + 2.0**-6).view(np.uint32)),
+                       dtype=np.uint64).astype(np.uint32) for v in (87.0, 86.6)]
+    x = np.concatenate([bits] + edges).view(np.float32)
+    x = np.concatenate([-np.abs(x), np.array([0.0, np.nan], np.float32)])
+    got, want = np.zeros_like(x), np.zeros_like(x)
+    gbdev._native.check(L.gbpt_fmath(5, x.ctypes.data, len(x), got.ctypes.data))
+    gbdev._native.check(L.gbpt_fmath(2, x.ctypes.data, len(x), want.ctypes.data))
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    finite = x[:4096 * 64]
+    assert np.array_equal(got[:len(finite)].view(np.uint32), orc.fmath("exp", finite).view(np.uint32))
+
+
 def test_philox_bitexact(gbdev, orc):
     L = gbdev._native.load()
     rng = np.random.Generator(np.random.PCG64(6))

@@ -179,8 +179,14 @@ def test_bilateral_kernel_bitexact(gbdev, orc):
     rng = np.random.Generator(np.random.PCG64(21))
     W, H = 77, 45
     planes = [rng.random(W * H * 3).astype(np.float32) for _ in range(4)]
+    # many equal neighbours (zero distances) and a few far outliers in the normal plane
+    planes[2] = np.round(planes[2] * 2.0).astype(np.float32) / np.float32(2.0)
+    planes[2][rng.integers(0, W * H * 3, 64)] = np.float32(1e6)
     L = gbdev._native.load()
-    for radius, emit, delta in ((4, False, 3.0), (5, True, 50.0), (2, False, 1.0)):
+    # radii 4 and 5 run the compile-time-radius tile kernels, 2/3/24 the run-time-radius one,
+    # 25 (window above the shared-memory limit) the direct kernel
+    for radius, emit, delta in ((4, False, 3.0), (5, True, 50.0), (2, False, 1.0), (4, True, 2.0), (5, False, 4.0),
+                                (3, True, 1.5), (24, False, 9.0), (25, True, 9.0)):
         g = np.zeros(64, np.float32)
         gbdev._native.check(L.gbpt_gaussian_table(delta, radius, g.ctypes.data))
         gref = orc.gaussian(delta, radius)

@@ -32,6 +32,34 @@ __device__ __forceinline__ void ldg_node(const float4* p, float4& a, float4& b) 
       : "l"(p));
 }
 
+// Three-input min / max (PTX ISA 8.8, sm_100 and later): one instruction each
+// for fminf(fminf(a, b), c) and fmaxf(fmaxf(a, b), c), NaN inputs ignored the
+// same way.
+__device__ __forceinline__ float fmin3_(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float fmax3_(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+// CURay::IntersectAABB (src/cudaRTCommon.cu:24-40) on the slab distances of
+// one box: true, with the entry distance tb (0 when the origin is inside),
+// when the box is hit and tb < limit.  The reference's test
+// `minmax >= maxmin && (minmax > 0 || maxmin > 0)` is written
+// `minmax >= maxmin && minmax > 0` (once maxmin <= minmax, maxmin > 0 implies
+// minmax > 0), and its walk's `0 <= tb` holds for every hit.
+__device__ __forceinline__ bool slab_hit(float t0x, float t1x, float t0y, float t1y, float t0z, float t1z,
+                                         float limit, float& tb) {
+  const float minmax = fmin3_(fmaxf(t0x, t1x), fmaxf(t0y, t1y), fmaxf(t0z, t1z));
+  const float maxmin = fmax3_(fminf(t0x, t1x), fminf(t0y, t1y), fminf(t0z, t1z));
+  tb = (maxmin > gb::kGtEps9) ? maxmin : 0.f;
+  return minmax >= maxmin && minmax > 0.f && tb < limit;
+}
+
 struct TraceHit {
   float t, w, u, v;
   uint32_t tri;
@@ -60,11 +88,8 @@ __device__ __forceinline__ bool trace_ref(const DevScene& S, gb::f3 o, gb::f3 d,
     const float t0x = (a.x - o.x) * inv.x, t1x = (b.x - o.x) * inv.x;
     const float t0y = (a.y - o.y) * inv.y, t1y = (b.y - o.y) * inv.y;
     const float t0z = (a.z - o.z) * inv.z, t1z = (b.z - o.z) * inv.z;
-    const float minmax = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-    const float maxmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
-    float tb = kInf;
-    if (minmax >= maxmin && (minmax > 0.f || maxmin > 0.f)) tb = (maxmin > kGtEps9) ? maxmin : 0.f;
-    if (!(tb >= 0.f && tb < minT)) continue;
+    float tb;
+    if (!slab_hit(t0x, t1x, t0y, t1y, t0z, t1z, minT, tb)) continue;
     const uint32_t off = __float_as_uint(a.w);
     const uint32_t tn = __float_as_uint(b.w);
     if (tn == 0) {
@@ -171,11 +196,8 @@ struct Walk {
     const float t0x = (a.x - o.x) * inv.x, t1x = (b.x - o.x) * inv.x;
     const float t0y = (a.y - o.y) * inv.y, t1y = (b.y - o.y) * inv.y;
     const float t0z = (a.z - o.z) * inv.z, t1z = (b.z - o.z) * inv.z;
-    const float minmax = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-    const float maxmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
-    float tb = kInf;
-    if (minmax >= maxmin && (minmax > 0.f || maxmin > 0.f)) tb = (maxmin > kGtEps9) ? maxmin : 0.f;
-    if (!(tb >= 0.f && tb < minT)) return false;
+    float tb;
+    if (!slab_hit(t0x, t1x, t0y, t1y, t0z, t1z, minT, tb)) return false;
     const uint32_t off = __float_as_uint(a.w);
     const uint32_t tn = __float_as_uint(b.w);
     if (tn == 0) {
@@ -264,11 +286,8 @@ struct Walk4 {
     const float t0x = (lx - o.x) * inv.x, t1x = (hx - o.x) * inv.x;
     const float t0y = (ly - o.y) * inv.y, t1y = (hy - o.y) * inv.y;
     const float t0z = (lz - o.z) * inv.z, t1z = (hz - o.z) * inv.z;
-    const float minmax = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-    const float maxmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
-    float tb = kInf;
-    if (minmax >= maxmin && (minmax > 0.f || maxmin > 0.f)) tb = (maxmin > kGtEps9) ? maxmin : 0.f;
-    return tb;
+    float tb;
+    return slab_hit(t0x, t1x, t0y, t1y, t0z, t1z, kInf, tb) ? tb : kInf;
   }
 
   template <bool kCount>

@@ -372,11 +372,13 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, uint32_t v
 // 5 resident CTAs per SM (48 registers) for the reference order: measured
 // 1-2% faster than 4 or 6 on the interior and hall workloads; 4 for the wide
 // walk (its wide-node step needs more registers).
-// walk steps per refill check: 2 in the wide order (+1-2%), 1 in the
-// reference order (2 measured 3-5% slower there)
+// walk steps per refill check (measured in Mpaths/s on interior / hall /
+// Cornell): reference order 1: 148.4 / 167.6 / 140.7, 2: 152.2 / 171.7 /
+// 144.5, 4: 154.9 / 174.3 / 143.1, 6: 156.0 / 176.2 / 141.9, 8: 155.5 /
+// 176.6 / 142.7; wide order 2: 170.0 / 180.7 / 159.2, 4: 171.2 / 181.8 / 157.4
 template <bool kWide>
 __host__ __device__ constexpr int walk_steps() {
-  return kWide ? 2 : 1;
+  return kWide ? 2 : 6;
 }
 
 template <bool kCount, bool kWide>
@@ -648,6 +650,13 @@ __global__ void __launch_bounds__(kBlock, 3) k_shade(DevScene S, FrameArgs a, Re
 // applied before the next bounce is shaded), so results are identical.
 enum : uint32_t { kIdle = 0, kPathExt = 1, kPathShadow = 2 };
 
+// walk steps of the tail kernel between two refill checks: a lane whose walk
+// ends early waits for the others, and the warp then shades its finished
+// paths together.  Measured in Mpaths/s on interior / Cornell: 1: 154.4 /
+// 144.2, 4: 157.5 / 158.7, 16: 161.1 / 171.4, 64: 162.3 / 189.1, 512: 156.7 /
+// 197.4 (the hall, depth 5, runs no tail kernel)
+__host__ __device__ constexpr int tail_steps() { return 64; }
+
 template <bool kCount, bool kWide>
 __global__ void __launch_bounds__(kBlock, 2) k_tail(DevScene S, FrameArgs a, RenderBuffers b, int in, int shIn,
                                                    uint32_t depth0, uint32_t kRefill) {
@@ -696,9 +705,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_tail(DevScene S, FrameArgs a, Ren
     }
     if (mode == kIdle) continue;
     const bool anyHit = mode == kPathShadow;
-    const bool done = kCount ? (anyHit ? w.template step<kCount>(S, stack, true, nnS, ntS)
-                                       : w.template step<kCount>(S, stack, false, nnE, ntE))
-                             : w.template step<kCount>(S, stack, anyHit, nnE, ntE);
+    bool done = false;
+#pragma unroll 1
+    for (int u = 0; u < tail_steps() && !done; u++)
+      done = kCount ? (anyHit ? w.template step<kCount>(S, stack, true, nnS, ntS)
+                              : w.template step<kCount>(S, stack, false, nnE, ntE))
+                    : w.template step<kCount>(S, stack, anyHit, nnE, ntE);
     if (!done) continue;
     if (anyHit) {
       shRays++;
@@ -1019,18 +1031,22 @@ void prepare_launches() {
 }
 
 uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested) {
-  // default, reference order: the last 4 bounces (measured on the 1024x768
-  // interior, depth 10: the tail kernel from bounce 6 beats both per-bounce
-  // launches throughout and earlier switches; its ~120 registers cost
-  // occupancy while many paths are alive).  Wide order: no tail (its walks
-  // are short enough that per-bounce launches win: 150.8 against 141.7
-  // Mpaths/s from bounce 6 and 124.0 from bounce 5).
+  // default, both orders: the tail kernel from bounce D/2 when D > 6, else
+  // per-bounce launches throughout.  Measured in Mpaths/s (reference / wide
+  // order) with 64 tail steps per refill check: interior, D = 10: from 4
+  // 165.3 / 162.6, from 5 166.1 / 172.2, from 6 162.1, from 7 151.5, no tail
+  // - / 170.1; Cornell, D = 8: from 4 194.6 / 174.4, from 5 182.6 / 165.9,
+  // no tail - / 159.8; hall, D = 5: no tail 176.7 / 180.6, from 3 158.9,
+  // from 2 147.1 (once few paths are alive the tail kernel's per-path
+  // schedule wins; while many are, per-bounce launches keep more of them
+  // resident: its ~120 registers cost occupancy).
+  (void)wide;
   static int v = [] {
     const char* e = std::getenv("GBPT_TAIL_FROM");
     return e ? std::atoi(e) : -2;
   }();
   if (requested >= 0) return (uint32_t)requested;
-  if (v == -2) return (!wide && eyeDepth > 6) ? eyeDepth - 4 : eyeDepth;
+  if (v == -2) return eyeDepth > 6 ? eyeDepth / 2 : eyeDepth;
   return v < 0 ? eyeDepth : (uint32_t)v;
 }
 

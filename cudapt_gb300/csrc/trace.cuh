@@ -114,7 +114,7 @@ __device__ __forceinline__ bool trace_ref(const DevScene& S, gb::f3 o, gb::f3 d,
       const f3 t = oe - mk(p0.x, p0.y, p0.z);
       const f3 te1 = cross(t, E0);
       const float rT = dot(te1, E1) * div;
-      if (rT < 0.f) continue;
+      if (!(rT >= 0.f && rT < minT)) continue;  // the acceptance test's bound, checked before u and v
       const float u = dot(de2, t) * div;
       if (u < 0.f || u > 1.f) continue;
       const float v = dot(te1, d) * div;
@@ -223,7 +223,7 @@ struct Walk {
       const f3 t = oe - mk(p0.x, p0.y, p0.z);
       const f3 te1 = cross(t, E0);
       const float rT = dot(te1, E1) * div;
-      if (rT < 0.f) continue;
+      if (!(rT >= 0.f && rT < minT)) continue;  // the acceptance test's bound, checked before u and v
       const float u = dot(de2, t) * div;
       if (u < 0.f || u > 1.f) continue;
       const float v = dot(te1, d) * div;
@@ -325,7 +325,7 @@ struct Walk4 {
         const f3 t = oe - mk(p0.x, p0.y, p0.z);
         const f3 te1 = cross(t, E0);
         const float rT = dot(te1, E1) * div;
-        if (rT < 0.f) continue;
+        if (!(rT >= 0.f && rT <= minT)) continue;  // the acceptance test's bound, checked before u and v
         const float u = dot(de2, t) * div;
         if (u < 0.f || u > 1.f) continue;
         const float v = dot(te1, d) * div;

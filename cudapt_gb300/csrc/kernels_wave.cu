@@ -654,11 +654,13 @@ enum : uint32_t { kIdle = 0, kPathExt = 1, kPathShadow = 2 };
 // ends early waits for the others, and the warp then shades its finished
 // paths together.  Measured in Mpaths/s on interior / Cornell: 1: 154.4 /
 // 144.2, 4: 157.5 / 158.7, 16: 161.1 / 171.4, 64: 162.3 / 189.1, 512: 156.7 /
-// 197.4 (the hall, depth 5, runs no tail kernel)
+// 197.4 (the hall, depth 5, runs no tail kernel).  Three CTAs per SM (80
+// registers, 80 B of spill) against two (116 registers): interior 167.0 ->
+// 170.0, Cornell 195.6 -> 193.6 Mpaths/s.
 __host__ __device__ constexpr int tail_steps() { return 64; }
 
 template <bool kCount, bool kWide>
-__global__ void __launch_bounds__(kBlock, 2) k_tail(DevScene S, FrameArgs a, RenderBuffers b, int in, int shIn,
+__global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, RenderBuffers b, int in, int shIn,
                                                    uint32_t depth0, uint32_t kRefill) {
   const uint32_t n = b.ctr->wave[in];
   const uint32_t cacheSize = b.ctr->cacheSize[a.cacheSel];

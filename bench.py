@@ -349,9 +349,9 @@ def l2_side(workload, trace_ms):
     if b is None or not trace_ms:
         return None
     return {"bytes_per_frame": b, "achieved_GBs": round(b / (trace_ms / 1e3) / 1e9, 1),
-            "throughput_pct_of_peak_ncu": [19.6, 15.6],
-            "note": "L2 serves the walks' node and triangle fetches that miss L1 (75% L1 hit rate); "
-                    "L2 throughput 16-20% of peak: latency-bound, not bandwidth-bound"}
+            "throughput_pct_of_peak_ncu": [21.5, 16.8],
+            "note": "L2 serves the walks' node and triangle fetches that miss L1 (74-75% L1 hit rate); "
+                    "L2 throughput 17-22% of peak: latency-bound, not bandwidth-bound"}
 
 
 def filter_roofline(phases, steps, np_, peak):

@@ -38,7 +38,7 @@ def rmse(a, b):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out", "learned_sampler.json"))
+    ap.add_argument("--out", default="learned_sampler.json")
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--res", default="320x180")
     ap.add_argument("--boxes", type=int, default=1200)

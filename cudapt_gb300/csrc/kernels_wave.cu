@@ -1033,22 +1033,20 @@ void prepare_launches() {
 }
 
 uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested) {
-  // default, both orders: the tail kernel from bounce D/2 when D > 6, else
-  // per-bounce launches throughout.  Measured in Mpaths/s (reference / wide
-  // order) with 64 tail steps per refill check: interior, D = 10: from 4
-  // 165.3 / 162.6, from 5 166.1 / 172.2, from 6 162.1, from 7 151.5, no tail
-  // - / 170.1; Cornell, D = 8: from 4 194.6 / 174.4, from 5 182.6 / 165.9,
-  // no tail - / 159.8; hall, D = 5: no tail 176.7 / 180.6, from 3 158.9,
-  // from 2 147.1 (once few paths are alive the tail kernel's per-path
-  // schedule wins; while many are, per-bounce launches keep more of them
-  // resident: its ~120 registers cost occupancy).
-  (void)wide;
+  // default when D > 6: the tail kernel from bounce D/2 - 1 in the reference
+  // order, D/2 in the wide order; per-bounce launches throughout for D <= 6.
+  // Measured in Mpaths/s (reference / wide order), tail kernel at three CTAs
+  // per SM: interior, D = 10: from 4 174.3 / 169.6, from 5 170.6 / 174.8,
+  // from 6 161.4 / 173.7; Cornell, D = 8: from 3 199.3 / 173.7, from 4 194.3
+  // / 173.5; hall, D = 5: no tail 176.7 / 180.5, from 4 171.1 / 175.8, from 3
+  // 158.9 (once few paths are alive the tail kernel's per-path schedule wins;
+  // while many are, per-bounce launches keep more of them resident).
   static int v = [] {
     const char* e = std::getenv("GBPT_TAIL_FROM");
     return e ? std::atoi(e) : -2;
   }();
   if (requested >= 0) return (uint32_t)requested;
-  if (v == -2) return eyeDepth > 6 ? eyeDepth / 2 : eyeDepth;
+  if (v == -2) return eyeDepth > 6 ? eyeDepth / 2 - (wide ? 0u : 1u) : eyeDepth;
   return v < 0 ? eyeDepth : (uint32_t)v;
 }
 

@@ -116,7 +116,8 @@ cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuff
 cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
                         uint32_t depth0, cudaStream_t st);
 // first bounce handled by the tail kernel: `requested` when >= 0 (>= D: none),
-// else GBPT_TAIL_FROM when set, else D/2 for D > 6 and none for D <= 6
+// else GBPT_TAIL_FROM when set, else D/2 - 1 (wide order: D/2) for D > 6 and
+// none for D <= 6
 uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested);
 // refill threshold of the persistent walks: `requested` when 1..32, else
 // GBPT_WALK_REFILL when set, else 8 (reference order) or 20 (wide order)

@@ -97,7 +97,7 @@ typedef struct gbpt_params {
   uint32_t walk_refill;     /* idle lanes of a warp that make a persistent walk fetch new rays
                                (1..32; 0: 8 in the reference order, 20 in the wide order) */
   int32_t tail_from;        /* first bounce the per-path tail kernel carries (>= the depth cap: none;
-                               -1: depth / 2 when the cap exceeds 6, else none) */
+                               -1: depth / 2 - 1 (wide order: depth / 2) when the cap exceeds 6, else none) */
 } gbpt_params;
 
 /* Renderer modes: the BDPT entries of the X-macro registry

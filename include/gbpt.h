@@ -268,10 +268,12 @@ gbpt_status gbpt_bilateral(const float* color, const float* pos, const float* no
  * cannot afford a cudaMalloc/cudaFree pair): the weight table g (host,
  * 2*radius+1 floats) is staged in a file-scope device array of 64 floats
  * instead of a per-call allocation, so radius must be <= 31.  The array is
- * shared by all calls on a device (calls that overlap on the GPU race on it)
- * and the first call on a device resolves its address; make that first call
- * before any stream capture.  stream may be NULL (default stream); the call
- * returns after the stream has finished the filter. */
+ * shared by all calls on a device (calls that overlap on the GPU race on it).
+ * The first call in a device's context resolves the array's address (again
+ * after cudaDeviceReset).  Each call copies g from host memory and then
+ * synchronizes the whole stream (all work queued on it, not only the
+ * filter), so it must not be made while the stream is being captured: it
+ * returns GBPT_ERR_STATE then.  stream may be NULL (default stream). */
 gbpt_status gbpt_bilateral_noalloc(const float* color, const float* pos, const float* norm, const float* emit,
                                    uint32_t width, uint32_t height, float color_eud, float pos_eud, float norm_eud,
                                    float emit_eud, uint32_t radius, const float* g, float* out, void* stream);

@@ -44,3 +44,16 @@ def camera_rays(cam, w, h, seed):
 def block_means(img, w, h, b=8):
     a = img.reshape(h, w, 3)[: h // b * b, : w // b * b]
     return a.reshape(h // b, b, w // b, b, 3).mean(axis=(1, 3))
+
+
+def assert_bits_equal(got, want, what=""):
+    """Exact equality of two float (or integer) arrays, word for word; the
+    message names how many words differ and the first few indices."""
+    g = np.ascontiguousarray(got)
+    w = np.ascontiguousarray(want)
+    assert g.shape == w.shape, (what, g.shape, w.shape)
+    gv = g.view(np.uint32) if g.dtype == np.float32 else g
+    wv = w.view(np.uint32) if w.dtype == np.float32 else w
+    bad = np.nonzero(gv.ravel() != wv.ravel())[0]
+    assert len(bad) == 0, (f"{what}: {len(bad)} of {gv.size} words differ; first at "
+                           f"{bad[:5].tolist()}: got {g.ravel()[bad[:5]].tolist()} want {w.ravel()[bad[:5]].tolist()}")

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from cudapt_gb300 import layouts
-from helpers import scene_arrays
+from helpers import assert_bits_equal, scene_arrays
 
 W = H = 48
 BILAT = layouts.MODE_BDPT_SC_BILAT
@@ -102,10 +102,6 @@ def _gpu(gb, frames, debug=0, **kw):
     return r, out
 
 
-def _same(a, b):
-    return np.mean(a.view(np.uint32) == b.view(np.uint32))
-
-
 @pytest.mark.gpu
 def test_gpu_bilat_planes_bitexact(gbdev, orc):
     frames = 6  # 4 traced + 2 filter-only
@@ -113,11 +109,9 @@ def test_gpu_bilat_planes_bitexact(gbdev, orc):
     ref, _, _ = _oracle(orc, frames)
     assert r.last_stats["paths"] == 0 and r.last_stats["frame"] == frames - 1
     for gid, oid in ((0, 0), (1, 1), (2, 2), (3, 3), (8, 8), (9, 9), (10, 10), (4, 4)):
-        got, want = r.read_buffer(gid), ref.get(oid)
-        assert _same(got, want) >= 0.998, (gid, _same(got, want))
-        np.testing.assert_allclose(got, want, rtol=1e-4, atol=1e-5)
+        assert_bits_equal(r.read_buffer(gid), ref.get(oid), f"plane {gid}")
     assert np.array_equal(out, r.read_buffer(4))
-    assert np.mean(r.read_buffer(6) == ref.sample_counts()[0]) >= 0.998
+    assert_bits_equal(r.read_buffer(6), ref.sample_counts()[0], "sampleN")
 
 
 @pytest.mark.gpu
@@ -125,9 +119,7 @@ def test_gpu_bilat_planes_bitexact(gbdev, orc):
 def test_gpu_bilat_debug_views(gbdev, orc, debug):
     r, out = _gpu(gbdev, 3, debug=debug, min_trace_prob=0.25)
     ref, _, _ = _oracle(orc, 3, debug=debug, min_trace_prob=0.25)
-    want = ref.get(11)
-    assert _same(out, want) >= 0.998, _same(out, want)
-    np.testing.assert_allclose(out, want, rtol=1e-4, atol=1e-5)
+    assert_bits_equal(out, ref.get(11), f"debug view {debug}")
 
 
 @pytest.mark.gpu

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from cudapt_gb300 import layouts
+from helpers import assert_bits_equal
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 PT = layouts.MODE_PT_SC
@@ -62,18 +63,16 @@ def _both(gb, orc, scene, W, H, frames, **kw):
 @pytest.mark.gpu
 def test_gpu_pt_glass_bitexact(gbdev, orc):
     r, ref, img, want = _both(gbdev, orc, _glass(), 64, 48, 5)
-    same = np.mean(img.view(np.uint32) == want.view(np.uint32))
-    assert same >= 0.995, same
-    np.testing.assert_allclose(img, want, rtol=1e-4, atol=1e-5)
+    assert_bits_equal(img, want, "image")
+    assert_bits_equal(r.read_buffer(6), ref.sample_counts()[0], "sampleN")
     st, rs = r.last_stats, ref.stats()
     assert st["shadow_rays"] == 0 and st["light_vertices"] == 0
-    assert abs(int(st["rays"]) - rs["ext_rays"]) <= 2e-3 * rs["ext_rays"]
-    assert abs(int(st["nodes"]) - rs["ext_nodes"]) <= 2e-3 * rs["ext_nodes"]
+    assert int(st["rays"]) == rs["ext_rays"] and int(st["nodes"]) == rs["ext_nodes"]
 
 
 @pytest.mark.gpu
 def test_gpu_pt_cornell_matches(gbdev, orc):
-    from helpers import scene_arrays
+    from helpers import assert_bits_equal, scene_arrays
     r, ref, img, want = _both(gbdev, orc, scene_arrays("cornell"), 64, 64, 4)
-    assert np.mean(img.view(np.uint32) == want.view(np.uint32)) >= 0.999
+    assert_bits_equal(img, want, "image")
     assert np.array_equal(r.read_buffer(6), np.full(64 * 64, 4, np.uint32))

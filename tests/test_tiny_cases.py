@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 from cudapt_gb300 import layouts, scenes
+from helpers import assert_bits_equal
 
 pytestmark = pytest.mark.gpu
 
@@ -34,5 +35,5 @@ def test_tiny_frames_match_oracle(gbdev, orc, mode, W, H):
     ref.render(orc.Scene(v, t, m), cam, 5)
     want = ref.get(0)
     assert np.isfinite(img).all()
-    np.testing.assert_allclose(img, want, rtol=1e-4, atol=1e-6)
-    np.testing.assert_array_equal(r.read_buffer(6), ref.sample_counts()[0])
+    assert_bits_equal(img, want, "image")
+    assert_bits_equal(r.read_buffer(6), ref.sample_counts()[0], "sampleN")

@@ -64,9 +64,12 @@ def test_noalloc_matches_allocating_entry_point(gbdev):
             b = dev.get(out_new, W * H * 3)
             assert np.isfinite(a).all()
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), f"call {call}"
-        # sizes beyond the 64-entry table are refused
-        with pytest.raises(gbdev.GbptError, match="radius"):
-            ck(L.gbpt_bilateral_noalloc(planes[0], planes[1], planes[2], None, 8, 8, 1.0, 1.0, 1.0, 1.0, 32,
-                                        g.ctypes.data, out_new, None))
+        # sizes beyond the 64-entry table are refused on the host, including radii
+        # whose 2*radius+1 wraps around in 32-bit arithmetic
+        for bad in (32, 0x80000000, 0xFFFFFFFF):
+            with pytest.raises(gbdev.GbptError, match="radius") as e:
+                ck(L.gbpt_bilateral_noalloc(planes[0], planes[1], planes[2], None, 8, 8, 1.0, 1.0, 1.0, 1.0, bad,
+                                            g.ctypes.data, out_new, None))
+            assert e.value.status == 1
     finally:
         dev.free()

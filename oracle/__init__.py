@@ -6,13 +6,17 @@ compiled from the sources in this folder by ``build()`` and loaded with
 ctypes.  Only tests/, ``__graft_entry__.smoke()`` and the CPU baseline of
 bench.py use it, always as the checker; the shipped library never loads it.
 
-Parity status: the reference cannot be compiled here (MSVC-only headers,
-legacy texture references), and its repository carries no tests, golden
-vectors or saved images for this path.  The oracle is pinned by the
-published Philox4x32-10 known-answer vectors, by hand-derived golden cases
-(tests/golden/) and by the BVH/traversal invariants the reference code
-implies; the estimator itself is "parity unpinned" against the reference
-binary.
+Parity status: pinned.  The reference's own BVH builder and traversal
+(src/bvhhelper.cpp, src/cudaRTCommon.cu) compile here from the checkout with
+the stand-ins of refpin/prelude.h (oracle/refpin, loaded by
+``oracle.refpin``); the oracle's BVH, intersection routines and
+TracePrimitive equal them to the bit (tests/test_refpin.py), and
+tests/golden/refpin_traces.npz carries their output to machines without the
+checkout.  The estimator above the traversal (shading, connections, the
+adaptive allocator, the filter) follows the reference line by line; its
+transcendentals are the project's own, and the reference's RNG (curand
+XORWOW) is replaced by Philox4x32-10, pinned by the published Random123
+known-answer vectors.
 """
 import ctypes
 import os
@@ -53,6 +57,8 @@ def lib():
             L.orc_scene_export.argtypes = [vp, vp, vp, vp, vp]
             L.orc_update_materials.argtypes = [vp, vp, u32]
             L.orc_trace.argtypes = [vp, vp, u32, f32, f32, i32, vp, vp, vp, vp, vp, vp, vp]
+            L.orc_intersect_aabb.argtypes = [vp, u32, vp]
+            L.orc_intersect_tri.argtypes = [vp, u32, f32, i32, vp]
             L.orc_default_params.argtypes = [vp]
             L.orc_renderer_create.restype = vp
             L.orc_renderer_create.argtypes = [u32, u32, i32, vp, u32]
@@ -198,6 +204,22 @@ class Renderer:
         out = np.zeros((max(n, 1), 21), np.float32)
         lib().orc_renderer_light_cache(self.h, _p(out))
         return out[:n]
+
+
+def intersect_aabb(cases):
+    """IntersectAABB over (n, 12) cases: origin, direction, min, max."""
+    cases = np.ascontiguousarray(cases, np.float32).reshape(-1, 12)
+    out = np.zeros(len(cases), np.float32)
+    lib().orc_intersect_aabb(_p(cases), len(cases), _p(out))
+    return out
+
+
+def intersect_tri(cases, eps=1e-9, cullback=True):
+    """IntersectTri over (n, 15) cases: origin, direction, p0, e0, e1; (n, 4) t, w, u, v."""
+    cases = np.ascontiguousarray(cases, np.float32).reshape(-1, 15)
+    out = np.zeros((len(cases), 4), np.float32)
+    lib().orc_intersect_tri(_p(cases), len(cases), eps, int(cullback), _p(out))
+    return out
 
 
 def render_fp64(scene, params, width, height, cam, frames, threads=None):

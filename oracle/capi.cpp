@@ -47,6 +47,22 @@ void orc_update_materials(void* sp, const void* mats, uint32_t nm) {
 }
 
 // rays: 6 floats each (origin, direction).  Outputs per ray.
+// IntersectAABB over n cases of 12 floats (origin, direction, min, max).
+void orc_intersect_aabb(const float* c, uint32_t n, float* out) {
+  for (uint32_t i = 0; i < n; i++) {
+    const float* q = c + (size_t)i * 12;
+    out[i] = intersect_aabb(q, q + 3, q + 6, q + 9);
+  }
+}
+
+// IntersectTri over n cases of 15 floats (origin, direction, p0, e0, e1); 4 floats out each (t, w, u, v).
+void orc_intersect_tri(const float* c, uint32_t n, float eps, int32_t cullback, float* out) {
+  for (uint32_t i = 0; i < n; i++) {
+    const float* q = c + (size_t)i * 15;
+    out[(size_t)i * 4] = intersect_tri(q, q + 3, q + 6, q + 9, q + 12, eps, cullback != 0, out + (size_t)i * 4 + 1);
+  }
+}
+
 void orc_trace(void* sp, const float* rays, uint32_t n, float maxDist, float eps, int32_t cullback, float* t,
                int32_t* triId, float* w, float* u, float* v, uint32_t* nodes, uint32_t* trisTested) {
   Scene* s = (Scene*)sp;

@@ -70,6 +70,9 @@ struct TraceCount {
 };
 
 // src/cudaRTCommon.cu:66-127 TracePrimitive
+float intersect_aabb(const float o[3], const float d[3], const float mn[3], const float mx[3]);
+float intersect_tri(const float o[3], const float d[3], const float p0[3], const float e0[3], const float e1[3],
+                    float eps, bool cullback, float wuv[3]);
 bool trace_primitive(const Scene& s, const float o[3], const float d[3], float maxDist, float eps, bool cullback,
                      Hit* hit, TraceCount* cnt);
 

@@ -129,6 +129,30 @@ bool trace_primitive(const Scene& s, const float o[3], const float d[3], float m
   return false;
 }
 
+// The two intersection routines alone, for case-by-case comparison with
+// the reference's CURay functions.
+float intersect_aabb(const float o[3], const float d[3], const float mn[3], const float mx[3]) {
+  RayPre r;
+  r.o = mk(o[0], o[1], o[2]);
+  r.d = mk(d[0], d[1], d[2]);
+  r.inv = vrcp(mk(escapeZero(r.d.x, kEpsF), escapeZero(r.d.y, kEpsF), escapeZero(r.d.z, kEpsF)));
+  return aabb(r, mk(mn[0], mn[1], mn[2]), mk(mx[0], mx[1], mx[2]));
+}
+
+float intersect_tri(const float o[3], const float d[3], const float p0[3], const float e0[3], const float e1[3],
+                    float eps, bool cullback, float wuv[3]) {
+  RayPre r;
+  r.o = mk(o[0], o[1], o[2]);
+  r.d = mk(d[0], d[1], d[2]);
+  float w = 0.f, u = 0.f, v = 0.f;
+  float t = tri_isect(r, mk(p0[0], p0[1], p0[2]), mk(e0[0], e0[1], e0[2]), mk(e1[0], e1[1], e1[2]), eps, cullback, w,
+                      u, v);
+  wuv[0] = w;
+  wuv[1] = u;
+  wuv[2] = v;
+  return t;
+}
+
 bool make_scene(const RTVertex* v, uint32_t nv, const RTTriangle* t, uint32_t nt, const RTMaterial* m, uint32_t nm,
                 Scene* s) {
   s->verts.assign(v, v + nv);

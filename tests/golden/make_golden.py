@@ -2,8 +2,8 @@
 
 Inputs:
   * the reference's own Cornell asset ``asset/model/cornell_box_with_sphere.obj``
-    (416 faces -> 792 triangles), read from the CudaPT checkout given on the
-    command line (default /root/reference), positions only;
+    (416 faces -> 792 triangles), read from the CudaPT checkout whose root
+    is the required command-line argument, positions only;
   * the 36-triangle procedural Cornell box of cudapt_gb300.scenes.
 
 Outputs (all produced by the CPU oracle, FP32 float contract):
@@ -97,4 +97,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_golden.py <CudaPT checkout root>")
+    main(sys.argv[1])

@@ -73,3 +73,62 @@ def test_golden_gpu(gbdev):
         img = r.render(s, cam)
         assert np.array_equal(img.view(np.uint32), d["frames"][f].view(np.uint32)), f
     assert np.array_equal(r.read_buffer(6), d["sampleN"])
+
+
+# ---- fixtures written from the reference's own code (make_refpin_golden.py) ----
+
+def _refpin_scenes():
+    from cudapt_gb300 import layouts
+    d = _load("refpin_traces.npz")
+    for name in d["names"]:
+        name = str(name)
+        pos, idx = d[f"{name}_pos"], d[f"{name}_idx"]
+        v = np.zeros(len(pos), layouts.VERTEX)
+        v["pos"] = pos
+        t = np.zeros(len(idx), layouts.TRIANGLE)
+        t["v0"], t["v1"], t["v2"] = idx[:, 0], idx[:, 1], idx[:, 2]
+        m = np.zeros(1, layouts.MATERIAL)
+        m[0] = layouts.material()
+        yield name, (v, t, m), d
+
+
+def test_refpin_fixture_oracle(orc):
+    """The oracle's BVH and TracePrimitive equal the reference's (fixture written
+    by the reference code compiled from its sources)."""
+    from helpers import assert_bits_equal
+    for name, (v, t, m), d in _refpin_scenes():
+        sc = orc.Scene(v, t, m)
+        b, o, order, _ = sc.export()
+        assert_bits_equal(b, d[f"{name}_bounds"], f"{name} bounds")
+        assert_bits_equal(o, d[f"{name}_off"], f"{name} offsets")
+        assert_bits_equal(order, d[f"{name}_order"], f"{name} order")
+        for k, (md, eps, cull) in enumerate(d["settings"]):
+            h = sc.trace(d[f"{name}_rays"], max_dist=float(md), eps=float(eps), cullback=bool(cull))
+            for key in ("t", "tri", "w", "u", "v"):
+                assert_bits_equal(h[key], d[f"{name}_s{k}_{key}"], f"{name} setting {k} {key}")
+
+
+def test_refpin_fixture_library_builder(gb):
+    """The library's threaded BVH builder equals the reference's CreateBVH +
+    InitialCompactBVH on the fixture scenes."""
+    from helpers import assert_bits_equal
+    for name, (v, t, m), d in _refpin_scenes():
+        b, o, order = gb.RTScene(v, t, m).build_bvh().bvh_export()
+        assert_bits_equal(b, d[f"{name}_bounds"], f"{name} bounds")
+        assert_bits_equal(o, d[f"{name}_off"], f"{name} offsets")
+        assert_bits_equal(order, d[f"{name}_order"], f"{name} order")
+
+
+@pytest.mark.gpu
+def test_refpin_fixture_gpu(gbdev):
+    """The GPU walk (gbpt_trace_rays) returns the reference TracePrimitive's hits
+    to the bit: closest hit, back-face culling and the shadow setting."""
+    from helpers import assert_bits_equal
+    for name, (v, t, m), d in _refpin_scenes():
+        s = gbdev.RTScene(v, t, m).build_bvh()
+        for k, (md, eps, cull) in enumerate(d["settings"]):
+            h = s.trace_rays(d[f"{name}_rays"], max_dist=float(md), eps=float(eps), cullback=bool(cull))
+            hit = d[f"{name}_s{k}_tri"] >= 0
+            assert_bits_equal(h["tri"], d[f"{name}_s{k}_tri"], f"{name} setting {k} tri")
+            for key in ("t", "w", "u", "v"):
+                assert_bits_equal(h[key][hit], d[f"{name}_s{k}_{key}"][hit], f"{name} setting {k} {key}")

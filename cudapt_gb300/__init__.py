@@ -9,7 +9,7 @@ import ctypes
 
 import numpy as np
 
-from . import layouts
+from . import _native, layouts
 from ._native import GbptError, Stats, as_c, check, load, ptr
 from .layouts import (MATERIAL, MODE_BDPT_SC, MODE_BDPT_SC_ADAP_BILAT, MODE_BDPT_SC_ADAP_BILAT_BINARY,
                       MODE_BDPT_SC_BILAT, MODE_PT_SC, PARAMS, TRIANGLE, VERTEX, default_params, material)
@@ -77,6 +77,22 @@ class RTScene:
     def update_materials(self, materials):
         self.materials = as_c(materials, MATERIAL)
         check(load().gbpt_scene_update_materials(self._h, ptr(self.materials), len(self.materials)))
+
+    def set_textures(self, textures):
+        """RTScene::m_pTextures: a list of (H, W, 4) float RGBA arrays (row 0
+        first), indexed by the materials' diffuseTexId / emissiveTexId."""
+        arrs = [np.ascontiguousarray(t, np.float32) for t in textures]
+        for a in arrs:
+            if a.ndim != 3 or a.shape[2] != 4:
+                raise ValueError("a texture is an (H, W, 4) float array")
+        rec = (_native.Texture * max(len(arrs), 1))()
+        for i, a in enumerate(arrs):
+            rec[i].rgba = a.ctypes.data
+            rec[i].width = a.shape[1]
+            rec[i].height = a.shape[0]
+        check(load().gbpt_scene_set_textures(self._h, ctypes.addressof(rec), len(arrs)))
+        self.textures = arrs  # kept for the caller's inspection; the library holds its own copy
+        return self
 
     def set_traversal(self, mode):
         """BVH walk order: 0 / "reference" (bit-exact with TracePrimitive, the default) or

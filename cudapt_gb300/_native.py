@@ -32,6 +32,11 @@ class GbptError(RuntimeError):
         self.status = status
 
 
+class Texture(ctypes.Structure):
+    """gbpt_texture: RTTexture (include/raytracer.h:219-226)."""
+    _fields_ = [("rgba", ctypes.c_void_p), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [
         ("frame", ctypes.c_uint32),
@@ -103,6 +108,7 @@ SIGNATURES = {
     "gbpt_scene_build_bvh": (i32, [vp, u32, u32, vp]),
     "gbpt_scene_update_materials": (i32, [vp, vp, u32]),
     "gbpt_scene_set_traversal": (i32, [vp, i32]),
+    "gbpt_scene_set_textures": (i32, [vp, vp, u32]),
     "gbpt_scene_bvh_info": (i32, [vp, vp, vp, vp]),
     "gbpt_scene_bvh_export": (i32, [vp, vp, vp, vp]),
     "gbpt_trace_rays": (i32, [vp, vp, u32, f32, f32, i32, vp, vp, vp, vp, vp, vp, vp, i32]),
@@ -156,6 +162,7 @@ SIGNATURES = {
     "gbpt_renderer_set_mlp": (i32, [vp, vp, i32]),
     "gbpt_renderer_features": (i32, [vp, vp, u32, i32, vp]),
     "gbpt_fmath": (i32, [i32, vp, u32, vp]),
+    "gbpt_texture_sample": (i32, [vp, u32, u32, vp, u32, i32, vp]),
     "gbpt_philox": (i32, [vp, u32, u32, u32, vp]),
 }
 

@@ -16,8 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgbpt.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels_wave.cu", "kernels_adapt.cu", "api.cu", "noalloc.cu", "image.cu", "mlp.cu", "bvh_build.cpp",
-           "server.cpp"]
+SOURCES = ["kernels_wave.cu", "kernels_adapt.cu", "api.cu", "noalloc.cu", "image.cu", "texture.cu", "mlp.cu",
+           "bvh_build.cpp", "server.cpp"]
 
 
 def _nvcc():

@@ -81,7 +81,15 @@ struct gbpt_scene {
   bool built = false;
   std::vector<gbpt_triangle> trisOrdered;
   std::vector<uint32_t> lightTri;
+  struct Texture {
+    std::vector<float4> texels;
+    uint32_t w = 0, h = 0;
+  };
+  std::vector<Texture> textures;  // RTScene::m_pTextures
   float4 *dNodes = nullptr, *dTris = nullptr, *dShade = nullptr, *dMats = nullptr, *dWide = nullptr;
+  float4* dTexels = nullptr;
+  uint4* dTexInfo = nullptr;
+  float2* dUvs = nullptr;
   uint32_t traversal = 0;  // 0: the reference's order, 1: wide (collapsed 4-ary tree)
   uint32_t* dLight = nullptr;
   DevScene dev;
@@ -96,6 +104,9 @@ struct gbpt_scene {
     dfree(dMats);
     dfree(dLight);
     dfree(dWide);
+    dfree(dTexels);
+    dfree(dTexInfo);
+    dfree(dUvs);
     dev = DevScene{};
   }
   ~gbpt_scene() { free_dev(); }
@@ -112,21 +123,75 @@ void scan_lights(gbpt_scene* s) {
   }
 }
 
+float as_f(uint32_t u) {
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+// material texture ids must index the scene's textures (negative: none)
+gbpt_status check_texture_ids(const std::vector<gbpt_material>& mats, size_t ntex) {
+  for (size_t i = 0; i < mats.size(); i++) {
+    const gbpt_material& a = mats[i];
+    for (int32_t id : {a.diffuseTexId, a.normalTexId, a.emissiveTexId})
+      if (id >= 0 && (size_t)id >= ntex)
+        return fail(GBPT_ERR_INVALID_ARG, "material " + std::to_string(i) + " names texture " + std::to_string(id) +
+                                              " but the scene has " + std::to_string(ntex) +
+                                              " (gbpt_scene_set_textures)");
+  }
+  return GBPT_OK;
+}
+
 std::vector<float4> pack_materials(const std::vector<gbpt_material>& mats) {
   std::vector<float4> m(mats.size() * 3);
   for (size_t i = 0; i < mats.size(); i++) {
     const gbpt_material& a = mats[i];
     m[3 * i] = make_float4(a.diffuse[0], a.diffuse[1], a.diffuse[2], a.transparency);
     m[3 * i + 1] = make_float4(a.emissive[0], a.emissive[1], a.emissive[2], a.specular);
-    m[3 * i + 2] = make_float4(a.metallic, a.roughness, 0.f, 0.f);
+    m[3 * i + 2] = make_float4(a.metallic, a.roughness, as_f((uint32_t)(a.diffuseTexId < 0 ? -1 : a.diffuseTexId)),
+                               as_f((uint32_t)(a.emissiveTexId < 0 ? -1 : a.emissiveTexId)));
   }
   return m;
 }
 
-float as_f(uint32_t u) {
-  float f;
-  std::memcpy(&f, &u, 4);
-  return f;
+// texels of every texture in one array, a {first texel, width, height} record
+// each, and the vertex uvs of every triangle in BVH order
+gbpt_status upload_textures(gbpt_scene* s) {
+  dfree(s->dTexels);
+  dfree(s->dTexInfo);
+  dfree(s->dUvs);
+  s->dev.texels = nullptr;
+  s->dev.texInfo = nullptr;
+  s->dev.uvs = nullptr;
+  if (s->textures.empty()) return GBPT_OK;
+  size_t total = 0;
+  std::vector<uint4> info(s->textures.size());
+  for (size_t i = 0; i < s->textures.size(); i++) {
+    info[i] = make_uint4((uint32_t)total, s->textures[i].w, s->textures[i].h, 0u);
+    total += s->textures[i].texels.size();
+  }
+  if (total >= 0xFFFFFFFFull) return fail(GBPT_ERR_INVALID_ARG, "textures exceed 2^32 texels in total");
+  const uint32_t nt = (uint32_t)s->trisOrdered.size();
+  std::vector<float2> uvs((size_t)nt * 3);
+  for (uint32_t i = 0; i < nt; i++) {
+    const gbpt_triangle& t = s->trisOrdered[i];
+    const gbpt_vertex* v[3] = {&s->verts[t.v0], &s->verts[t.v1], &s->verts[t.v2]};
+    for (int k = 0; k < 3; k++) uvs[3 * (size_t)i + k] = make_float2(v[k]->tex[0], v[k]->tex[1]);
+  }
+  CK(dalloc(&s->dTexels, total));
+  CK(dalloc(&s->dTexInfo, info.size()));
+  CK(dalloc(&s->dUvs, uvs.size()));
+  size_t off = 0;
+  for (const auto& t : s->textures) {
+    CK(cudaMemcpy(s->dTexels + off, t.texels.data(), t.texels.size() * 16, cudaMemcpyHostToDevice));
+    off += t.texels.size();
+  }
+  CK(cudaMemcpy(s->dTexInfo, info.data(), info.size() * 16, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->dUvs, uvs.data(), uvs.size() * 8, cudaMemcpyHostToDevice));
+  s->dev.texels = s->dTexels;
+  s->dev.texInfo = s->dTexInfo;
+  s->dev.uvs = s->dUvs;
+  return GBPT_OK;
 }
 
 gbpt_status upload_wide(gbpt_scene* s) {
@@ -140,6 +205,8 @@ gbpt_status upload_wide(gbpt_scene* s) {
 }
 
 gbpt_status upload_scene(gbpt_scene* s) {
+  gbpt_status ids = check_texture_ids(s->mats, s->textures.size());
+  if (ids != GBPT_OK) return ids;
   s->free_dev();
   const uint32_t nt = (uint32_t)s->trisOrdered.size(), nn = s->bvh.nodeN;
   // one all-zero node record and one all-zero triangle record after the
@@ -190,6 +257,8 @@ gbpt_status upload_scene(gbpt_scene* s) {
     gbpt_status w = upload_wide(s);
     if (w != GBPT_OK) return w;
   }
+  gbpt_status tx = upload_textures(s);
+  if (tx != GBPT_OK) return tx;
   s->uploaded = true;
   return GBPT_OK;
 }
@@ -1021,6 +1090,11 @@ gbpt_status gbpt_scene_update_materials(gbpt_scene* s, const gbpt_material* mats
   scan_lights(s);
   s->version = next_version();  // progressive accumulation restarts (src/cudaRTBDPTStream.cu:845-850)
   if (!s->uploaded) return GBPT_OK;
+  gbpt_status ids = check_texture_ids(s->mats, s->textures.size());
+  if (ids != GBPT_OK) {
+    s->uploaded = false;  // the next use uploads again and reports the bad id
+    return ids;
+  }
   std::vector<float4> m = pack_materials(s->mats);
   CK(cudaMemcpy(s->dMats, m.data(), m.size() * 16, cudaMemcpyHostToDevice));
   dfree(s->dLight);
@@ -1029,6 +1103,24 @@ gbpt_status gbpt_scene_update_materials(gbpt_scene* s, const gbpt_material* mats
     CK(cudaMemcpy(s->dLight, s->lightTri.data(), s->lightTri.size() * 4, cudaMemcpyHostToDevice));
   s->dev.lightTri = s->dLight;
   s->dev.lightN = (uint32_t)s->lightTri.size();
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_scene_set_textures(gbpt_scene* s, const gbpt_texture* tex, uint32_t n) {
+  if (!s || (n && !tex)) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  std::vector<gbpt_scene::Texture> t(n);
+  for (uint32_t i = 0; i < n; i++) {
+    if (!tex[i].rgba || tex[i].width == 0 || tex[i].height == 0 || tex[i].width > 65536 || tex[i].height > 65536)
+      return fail(GBPT_ERR_INVALID_ARG, "texture " + std::to_string(i) + " is empty, NULL or above 65536 texels a side");
+    t[i].w = tex[i].width;
+    t[i].h = tex[i].height;
+    t[i].texels.resize((size_t)tex[i].width * tex[i].height);
+    std::memcpy(t[i].texels.data(), tex[i].rgba, t[i].texels.size() * 16);
+  }
+  std::lock_guard<std::mutex> lock(s->upload);
+  s->textures.swap(t);
+  s->version = next_version();  // progressive accumulation restarts
+  s->uploaded = false;          // the next use uploads the scene with its textures
   return GBPT_OK;
 }
 

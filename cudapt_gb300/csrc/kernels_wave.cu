@@ -27,6 +27,7 @@
 
 #include "launch.h"
 #include "shade.cuh"
+#include "texture.cuh"
 #include "trace.cuh"
 
 namespace gbpt {
@@ -50,6 +51,7 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 struct Mat {
   f3 diff, emis;
   float trans, spec, metal, rough;
+  int32_t texD, texE;  // diffuseTexId, emissiveTexId (-1: none)
 };
 __device__ __forceinline__ Mat load_mat(const DevScene& S, uint32_t id) {
   float4 a = __ldg(S.mats + 3 * (size_t)id), b = __ldg(S.mats + 3 * (size_t)id + 1),
@@ -61,6 +63,36 @@ __device__ __forceinline__ Mat load_mat(const DevScene& S, uint32_t id) {
   m.spec = b.w;
   m.metal = c.x;
   m.rough = c.y;
+  m.texD = __float_as_int(c.z);
+  m.texE = __float_as_int(c.w);
+  return m;
+}
+
+// The texture half of GetMaterialColors (src/cudaRTCommon.cu:369-406) at the
+// barycentrics (w, u, v) of triangle `tri`: uv = ((uv0*w) + (uv1*u)) + uv2*v
+// (the float2 operators of the reference's kernels, e.g.
+// src/cudaRTBDPTStream.cu:379-382); a diffuse texture gives the diffuse
+// colour and scales the transparency by its alpha, an emissive texture gives
+// the emissive colour.
+__device__ __forceinline__ void apply_textures(const DevScene& S, Mat& m, uint32_t tri, float w, float u, float v) {
+  const float2* q = S.uvs + 3 * (size_t)tri;
+  const float2 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+  const float tu = (a.x * w + b.x * u) + c.x * v;
+  const float tv = (a.y * w + b.y * u) + c.y * v;
+  if (m.texD >= 0) {
+    const float4 t = tex_bilinear(S.texels, __ldg(S.texInfo + m.texD), tu, tv);
+    m.diff = mk(t.x, t.y, t.z);
+    m.trans = t.w * m.trans;
+  }
+  if (m.texE >= 0) {
+    const float4 t = tex_bilinear(S.texels, __ldg(S.texInfo + m.texE), tu, tv);
+    m.emis = mk(t.x, t.y, t.z);
+  }
+}
+__device__ __forceinline__ Mat load_mat_at(const DevScene& S, uint32_t matId, uint32_t tri, float w, float u,
+                                           float v) {
+  Mat m = load_mat(S, matId);
+  if (m.texD >= 0 || m.texE >= 0) apply_textures(S, m, tri, w, u, v);
   return m;
 }
 
@@ -219,7 +251,7 @@ __global__ void __launch_bounds__(1024) k_light(DevScene S, FrameArgs a, float4*
     }
     float lvv = 1.f - lw - lu;
     Surf sf = load_surf(S, S.lightTri[id], lw, lu, lvv, true);
-    Mat m = load_mat(S, sf.mat);
+    Mat m = load_mat_at(S, sf.mat, S.lightTri[id], lw, lu, lvv);
     dir = cos_dir(u[3], u[4], sf.norm);
     orig = sf.pos + kBias * sf.norm;
     sample = m.emis;
@@ -267,7 +299,7 @@ __global__ void __launch_bounds__(1024) k_light(DevScene S, FrameArgs a, float4*
           draw8(a.key0, a.key1, x, a.frame, kLightBounce, depth, 0, u);
           float hw = 1.f - h.u - h.v;
           Surf sf = load_surf(S, h.tri, hw, h.u, h.v, true);
-          Mat m = load_mat(S, sf.mat);
+          Mat m = load_mat_at(S, sf.mat, h.tri, hw, h.u, h.v);
           Bounce B;
           sample_bounce(orig, dir, h.t, sf.norm, m, u, false, false, false, B);
           LV v;
@@ -511,7 +543,7 @@ __device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a
   draw8(a.key0, a.key1, pix, a.frame, kEyeBounce, depth, smp, u);
   const float hu = h4.z, hv = h4.w, hw = 1.f - hu - hv;
   Surf sf = load_surf(S, __float_as_uint(h4.y), hw, hu, hv, a.gbuffer && depth == 0);
-  Mat m = load_mat(S, sf.mat);
+  Mat m = load_mat_at(S, sf.mat, __float_as_uint(h4.y), hw, hu, hv);
   Bounce B;
   sample_bounce(orig, dir, h4.x, sf.norm, m, u, a.specPush != 0, a.bilat != 0, a.ptsc != 0, B);
   pathSample = pathSample + vmul(m.emis, outMul);

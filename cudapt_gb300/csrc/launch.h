@@ -14,7 +14,8 @@ namespace gbpt {
 //   {n0.xyz, p0.x} {n1.xyz, p0.y} {n2.xyz, p0.z} {p1.xyz, mat} {p2.xyz, 0}
 // so a hit reads one contiguous record instead of RTTriangle + 3 RTVertex.
 // Materials: {diffuse.xyz, transparency} {emissive.xyz, specular}
-//            {metallic, roughness, 0, 0}.
+//            {metallic, roughness, diffuseTexId, emissiveTexId} (ids as int
+//            bits, -1: none).
 //
 // Wide traversal (opt-in, gbpt_scene_set_traversal): the same tree collapsed
 // to 4 children per node (each node's children are its binary grandchildren,
@@ -30,6 +31,12 @@ struct DevScene {
   const float4* mats = nullptr;
   const uint32_t* lightTri = nullptr;
   const float4* wide = nullptr;  // collapsed 4-wide tree (wide traversal only)
+  // material textures (only when the scene has any): texels of every texture,
+  // one {first texel, width, height, 0} record per texture, and the three
+  // vertex uvs of each triangle in BVH order
+  const float4* texels = nullptr;
+  const uint4* texInfo = nullptr;
+  const float2* uvs = nullptr;
   uint32_t nodeN = 0, triN = 0, lightN = 0, matN = 0;
   uint32_t wideN = 0;
   uint32_t traversal = 0;        // 0: the reference's order (default), 1: wide

@@ -50,6 +50,13 @@ typedef struct gbpt_material { /* RTMaterial (no FULLSPECTRAL), 80 bytes */
   float anisotropic, sheen, sheenTint, clearcoat, clearcoatGloss;
 } gbpt_material;
 
+/* RTTexture (include/raytracer.h:219-226): width*height texels of 4 floats
+ * (RGBA), row-major, row 0 first. */
+typedef struct gbpt_texture {
+  const float* rgba;
+  uint32_t width, height;
+} gbpt_texture;
+
 /* Camera of RTRenderer::Render(camPos, camDir, camUp, fov, scene)
  * (include/raytracer.h:310); fov in radians. */
 typedef struct gbpt_camera {
@@ -166,6 +173,21 @@ gbpt_status gbpt_scene_build_bvh(gbpt_scene* s, uint32_t max_depth, uint32_t thr
  * origin push; node counts differ.  Restarts progressive accumulation. */
 gbpt_status gbpt_scene_set_traversal(gbpt_scene* s, int32_t traversal);
 gbpt_status gbpt_scene_update_materials(gbpt_scene* s, const gbpt_material* mats, uint32_t nm);
+/* The scene's textures, RTScene::m_pTextures (include/raytracer.h:228-290,
+ * filled by AssimpProcessSceneMaterial's texture loader, src/raytracer.cpp:
+ * 180-195), copied; they replace any set before.  A material's
+ * diffuseTexId / emissiveTexId index them: GetMaterialColors
+ * (src/cudaRTCommon.cu:369-406) then takes the diffuse colour from the
+ * texture's RGB and multiplies the transparency by its alpha, or takes the
+ * emissive colour from the texture's RGB, at the hit's interpolated vertex
+ * uv.  Sampling follows the reference's texture descriptor
+ * (src/cudaRTCommon.cu:418-448: normalized coordinates, wrap, linear
+ * filtering with 8-bit weights), evaluated in the kernels.  normalTexId is
+ * fetched but unused by the reference and is ignored here.  A material whose
+ * texture id is not below the texture count makes the next upload (first
+ * render or trace) fail with GBPT_ERR_INVALID_ARG.  Restarts progressive
+ * accumulation. */
+gbpt_status gbpt_scene_set_textures(gbpt_scene* s, const gbpt_texture* tex, uint32_t n);
 /* CompactBVH export (include/bvhhelper.h:45-54): node count first (pass NULL
  * arrays), then bounds[6*nodeN] (min xyz, max xyz), offOrTSTN[2*nodeN],
  * tri_order[nt] (CreateBVH's return value). */
@@ -420,6 +442,13 @@ gbpt_status gbpt_test_fail_allocations(int64_t after);
  * which: 0 sin, 1 cos, 2 exp, 3 round-down sqrt, 4 x^5, 5 exp of an argument <= 0 as the
  * bilateral filter's tile kernel evaluates it (equal to 2 there). */
 gbpt_status gbpt_fmath(int32_t which, const float* x, uint32_t n, float* out);
+/* Test utility (allocates): n float4 samples of one RGBA float texture at the
+ * n (u, v) pairs of uv, either through the texture unit (hardware = 1: a
+ * texture object with CreateCURTTexture's descriptor, src/cudaRTCommon.cu:
+ * 418-448) or through the kernels' software filter (hardware = 0); host
+ * arrays. */
+gbpt_status gbpt_texture_sample(const float* rgba, uint32_t width, uint32_t height, const float* uv, uint32_t n,
+                                int32_t hardware, float* out);
 /* Philox4x32-10 by a kernel: n counters (4 words each) -> 4 words each, host arrays. */
 gbpt_status gbpt_philox(const uint32_t* ctr, uint32_t n, uint32_t k0, uint32_t k1, uint32_t* out);
 

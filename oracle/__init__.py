@@ -58,6 +58,9 @@ def lib():
             L.orc_update_materials.argtypes = [vp, vp, u32]
             L.orc_trace.argtypes = [vp, vp, u32, f32, f32, i32, vp, vp, vp, vp, vp, vp, vp]
             L.orc_intersect_aabb.argtypes = [vp, u32, vp]
+            L.orc_scene_set_textures.argtypes = [vp, u32, vp, vp, vp]
+            L.orc_texture_sample.argtypes = [vp, u32, u32, vp, u32, vp]
+            L.orc_material_colors.argtypes = [vp, vp, u32, u32, vp, vp, vp, vp]
             L.orc_intersect_tri.argtypes = [vp, u32, f32, i32, vp]
             L.orc_default_params.argtypes = [vp]
             L.orc_renderer_create.restype = vp
@@ -133,6 +136,15 @@ class Scene:
     def update_materials(self, mats):
         self.mats = mats
         lib().orc_update_materials(self.h, _p(mats), len(mats))
+
+    def set_textures(self, textures):
+        """RTScene::m_pTextures: (H, W, 4) float RGBA arrays, row 0 first."""
+        arrs = [np.ascontiguousarray(t, np.float32) for t in textures]
+        w = np.array([a.shape[1] for a in arrs], np.uint32)
+        h = np.array([a.shape[0] for a in arrs], np.uint32)
+        flat = np.concatenate([a.reshape(-1) for a in arrs]) if arrs else np.zeros(1, np.float32)
+        lib().orc_scene_set_textures(self.h, len(arrs), _p(w), _p(h), _p(flat))
+        self.textures = arrs
 
     def trace(self, rays, max_dist=1e20, eps=1e-9, cullback=False):
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
@@ -219,6 +231,29 @@ def intersect_tri(cases, eps=1e-9, cullback=True):
     cases = np.ascontiguousarray(cases, np.float32).reshape(-1, 15)
     out = np.zeros((len(cases), 4), np.float32)
     lib().orc_intersect_tri(_p(cases), len(cases), eps, int(cullback), _p(out))
+    return out
+
+
+def texture_sample(rgba, uv):
+    """The linear-filtered, wrapped fetch of an (H, W, 4) texture at (n, 2) uv (texture_ref.h)."""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    out = np.zeros((len(uv), 4), np.float32)
+    lib().orc_texture_sample(_p(rgba), rgba.shape[1], rgba.shape[0], _p(uv), len(uv), _p(out))
+    return out
+
+
+def material_colors(mat, uv, textures):
+    """GetMaterialColors' colours of one MATERIAL record at (n, 2) uv with
+    (H, W, 4) textures: (n, 8) = diffuse, emissive, transparency, 0."""
+    arrs = [np.ascontiguousarray(t, np.float32) for t in textures]
+    w = np.array([a.shape[1] for a in arrs] or [0], np.uint32)
+    h = np.array([a.shape[0] for a in arrs] or [0], np.uint32)
+    flat = np.concatenate([a.reshape(-1) for a in arrs]) if arrs else np.zeros(1, np.float32)
+    m = np.ascontiguousarray(np.asarray(mat).reshape(()))
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    out = np.zeros((len(uv), 8), np.float32)
+    lib().orc_material_colors(m.ctypes.data, _p(uv), len(uv), len(arrs), _p(w), _p(h), _p(flat), _p(out))
     return out
 
 

@@ -220,11 +220,36 @@ struct MatV {
   const RTMaterial* m;
 };
 
+// diff / emissive / trans: GetMaterialColors (src/cudaRTCommon.cu:369-406)
+// at the hit's uv = ((uv0*w) + (uv1*u)) + uv2*v (the reference's float2
+// operators, src/cudaRTBDPTStream.cu:379-382): a diffuse texture replaces the
+// diffuse colour and scales the transparency by its alpha, an emissive
+// texture replaces the emissive colour (texture_ref.h).
 template <typename R>
 struct HitShade {
   V<R> norm, triPos;
   const RTMaterial* mat;
+  V<R> diff, emissive;
+  R trans;
 };
+
+template <typename R>
+static inline void mat_colors(const std::vector<Texture>& texs, const RTMaterial& m, R tu, R tv, V<R>& diff,
+                              V<R>& emissive, R& trans) {
+  diff = ld<R>(m.diffuse);
+  emissive = ld<R>(m.emissive);
+  trans = (R)m.transparency;
+  R tx[4];
+  if (m.diffuseTexId >= 0 && (size_t)m.diffuseTexId < texs.size()) {
+    tex_bilinear<R>(texs[(size_t)m.diffuseTexId], tu, tv, tx);
+    diff = mkv<R>(tx[0], tx[1], tx[2]);
+    trans = tx[3] * trans;
+  }
+  if (m.emissiveTexId >= 0 && (size_t)m.emissiveTexId < texs.size()) {
+    tex_bilinear<R>(texs[(size_t)m.emissiveTexId], tu, tv, tx);
+    emissive = mkv<R>(tx[0], tx[1], tx[2]);
+  }
+}
 
 template <typename R>
 static inline HitShade<R> hit_shade(const Scene& s, int32_t triId, R w, R u, R v) {
@@ -236,8 +261,34 @@ static inline HitShade<R> hit_shade(const Scene& s, int32_t triId, R w, R u, R v
   h.norm = (ld<R>(a.norm) * w + ld<R>(b.norm) * u) + ld<R>(c.norm) * v;
   h.triPos = (ld<R>(a.pos) * w + ld<R>(b.pos) * u) + ld<R>(c.pos) * v;
   h.mat = &s.mats[t.mat];
+  const RTMaterial& m = *h.mat;
+  R tu = 0, tv = 0;
+  if (m.diffuseTexId >= 0 || m.emissiveTexId >= 0) {
+    tu = ((R)a.tex[0] * w + (R)b.tex[0] * u) + (R)c.tex[0] * v;
+    tv = ((R)a.tex[1] * w + (R)b.tex[1] * u) + (R)c.tex[1] * v;
+  }
+  mat_colors<R>(s.textures, m, tu, tv, h.diff, h.emissive, h.trans);
   return h;
 }
+
+}  // namespace
+
+// GetMaterialColors' colour outputs for one material at n uvs: 8 floats each
+// (diffuse rgb, emissive rgb, transparency, 0).
+void material_colors(const std::vector<Texture>& texs, const RTMaterial& m, const float* uv, uint32_t n, float* out) {
+  for (uint32_t i = 0; i < n; i++) {
+    V<float> d, e;
+    float tr;
+    mat_colors<float>(texs, m, uv[2 * i], uv[2 * i + 1], d, e, tr);
+    float* o = out + 8 * (size_t)i;
+    o[0] = d.x; o[1] = d.y; o[2] = d.z;
+    o[3] = e.x; o[4] = e.y; o[5] = e.z;
+    o[6] = tr;
+    o[7] = 0.f;
+  }
+}
+
+namespace {
 
 // double-precision walk of the same tree (FP64 mode only)
 struct HitD {
@@ -404,8 +455,8 @@ static void eye_path(const Scene& s, const Params& p, const LightVertex* cache, 
     draw8(p.seed, p.request_id, pathId, frame, kEyeBounce, depth, sample, u);
     HitShade<R> hs = hit_shade<R>(s, hit.triId, hit.w, hit.u, hit.v);
     const RTMaterial& m = *hs.mat;
-    V<R> diff = ld<R>(m.diffuse), emissive = ld<R>(m.emissive);
-    R trans = (R)m.transparency, specular = (R)m.specular, metallic = (R)m.metallic, rough = (R)m.roughness;
+    V<R> diff = hs.diff, emissive = hs.emissive;
+    R trans = hs.trans, specular = (R)m.specular, metallic = (R)m.metallic, rough = (R)m.roughness;
     V<R> norm = hs.norm;
     V<R> nl = dotv(norm, dir) < (R)0 ? norm : (R)-1 * norm;
     V<R> hDir = ggx_sample<R>((R)u[0], (R)u[1], rough, nl);
@@ -582,19 +633,19 @@ static void light_pass_f(const Scene& s, const Params& p, uint32_t frame, std::v
     lp.orig = hs.triPos + K<float>::bias * hs.norm;
     lp.dir = dd;
     lp.outMul = mkv<float>(1, 1, 1);
-    lp.sample = ld<float>(m.emissive);
+    lp.sample = hs.emissive;
     lp.home = x;
     lp.depth = 0;
     lp.type = kLight;
     lp.id = x;
     stream.push_back(lp);
     LightVertex& lv = cache[x];
-    st(lv.irrad, ld<float>(m.emissive));
+    st(lv.irrad, hs.emissive);
     st(lv.irradDir, mkv<float>(0, 0, 0));
     st(lv.norm, hs.norm);
     st(lv.pos, hs.triPos);
-    st(lv.diff, ld<float>(m.diffuse));
-    st(lv.emissive, ld<float>(m.emissive));
+    st(lv.diff, hs.diff);
+    st(lv.emissive, hs.emissive);
     lv.specular = m.specular;
     lv.metallic = m.metallic;
     lv.roughness = m.roughness;
@@ -615,8 +666,8 @@ static void light_pass_f(const Scene& s, const Params& p, uint32_t frame, std::v
       draw8(p.seed, p.request_id, lp.id, frame, kLightBounce, lp.depth, 0, u);
       HitShade<float> hs = hit_shade<float>(s, hit.triId, hit.w, hit.u, hit.v);
       const RTMaterial& m = *hs.mat;
-      V<float> diff = ld<float>(m.diffuse), emissive = ld<float>(m.emissive);
-      float trans = m.transparency, specular = m.specular, metallic = m.metallic, rough = m.roughness;
+      V<float> diff = hs.diff, emissive = hs.emissive;
+      float trans = hs.trans, specular = m.specular, metallic = m.metallic, rough = m.roughness;
       V<float> norm = hs.norm, dir = lp.dir;
       V<float> nl = dotv(norm, dir) < 0.f ? norm : -1.f * norm;
       st(slot.irrad, lp.sample);

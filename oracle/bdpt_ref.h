@@ -96,6 +96,10 @@ void light_pass(Renderer* r, const Scene& s, uint32_t frame);
 void render_fp64(const Scene& s, const Params& p, uint32_t W, uint32_t H, const Camera& cam, uint32_t frames,
                  uint32_t threads, double* out);
 
+// GetMaterialColors (src/cudaRTCommon.cu:369-406), colour outputs at n uvs:
+// 8 floats each (diffuse rgb, emissive rgb, transparency, 0)
+void material_colors(const std::vector<Texture>& texs, const RTMaterial& m, const float* uv, uint32_t n, float* out);
+
 // src/cudaBilateralFilter.cu:5-24 and :66-142 (posnorm / posnormemit)
 void gaussian_table(float delta, uint32_t radius, float* g);
 void bilateral(const float* color, const float* pos, const float* norm, const float* emit, uint32_t W, uint32_t H,

@@ -46,6 +46,46 @@ void orc_update_materials(void* sp, const void* mats, uint32_t nm) {
   refresh_lights(s);
 }
 
+// n textures: widths / heights, texels of all of them concatenated (4 floats each).
+void orc_scene_set_textures(void* sp, uint32_t n, const uint32_t* w, const uint32_t* h, const float* rgba) {
+  Scene* s = (Scene*)sp;
+  s->textures.assign(n, Texture{});
+  size_t off = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    Texture& t = s->textures[i];
+    t.w = w[i];
+    t.h = h[i];
+    const size_t cnt = (size_t)w[i] * h[i] * 4;
+    t.rgba.assign(rgba + off, rgba + off + cnt);
+    off += cnt;
+  }
+}
+
+// n texture samples (u, v) of one texture -> 4 floats each (texture_ref.h)
+void orc_texture_sample(const float* rgba, uint32_t w, uint32_t h, const float* uv, uint32_t n, float* out) {
+  Texture t;
+  t.w = w;
+  t.h = h;
+  t.rgba.assign(rgba, rgba + (size_t)w * h * 4);
+  for (uint32_t i = 0; i < n; i++) tex_bilinear<float>(t, uv[2 * i], uv[2 * i + 1], out + 4 * (size_t)i);
+}
+
+// GetMaterialColors of one material at n uvs with the given textures
+// (widths / heights / concatenated texels as orc_scene_set_textures).
+void orc_material_colors(const void* mat, const float* uv, uint32_t n, uint32_t ntex, const uint32_t* w,
+                         const uint32_t* h, const float* rgba, float* out) {
+  std::vector<Texture> texs(ntex);
+  size_t off = 0;
+  for (uint32_t i = 0; i < ntex; i++) {
+    texs[i].w = w[i];
+    texs[i].h = h[i];
+    const size_t cnt = (size_t)w[i] * h[i] * 4;
+    texs[i].rgba.assign(rgba + off, rgba + off + cnt);
+    off += cnt;
+  }
+  material_colors(texs, *(const RTMaterial*)mat, uv, n, out);
+}
+
 // rays: 6 floats each (origin, direction).  Outputs per ray.
 // IntersectAABB over n cases of 12 floats (origin, direction, min, max).
 void orc_intersect_aabb(const float* c, uint32_t n, float* out) {

@@ -8,6 +8,8 @@
 #include <cstdint>
 #include <vector>
 
+#include "texture_ref.h"
+
 namespace orc {
 
 struct BuildStats {
@@ -54,6 +56,7 @@ struct Scene {
   BVH bvh;
   std::vector<float> isect;  // 9 floats per triangle: p0, e0, e1
   std::vector<uint32_t> lightTri;
+  std::vector<Texture> textures;  // RTScene::m_pTextures
 };
 
 bool make_scene(const RTVertex* v, uint32_t nv, const RTTriangle* t, uint32_t nt, const RTMaterial* m, uint32_t nm,

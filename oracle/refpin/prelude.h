@@ -28,9 +28,9 @@
 //     tex1Dfetch, cudaBindTexture) become a plain array view; a fetch beyond
 //     the bound range returns zeros as a texture reference did.
 //   * tex2D on a texture object (GetMaterialColors) reads a host texture
-//     registered by the pin library (refpin_capi.cpp), filtered as the
-//     reference's texture descriptor asks (normalized coordinates, wrap,
-//     linear filtering with 8-bit fractional weights).
+//     registered by the pin library (refpin_capi.cpp) through the oracle's
+//     restatement of the descriptor's filter (oracle/texture_ref.h:
+//     normalized coordinates, wrap, linear filtering with 8-bit weights).
 //   * curand_kernel.h, warp intrinsics and atomics are declared only so that
 //     the file compiles; the pin library never calls the functions that use
 //     them.

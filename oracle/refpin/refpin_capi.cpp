@@ -12,6 +12,7 @@
 // the three texture references).  One scene is bound at a time.
 #include "bvhhelper.h"
 #include "cudaRTCommon.h"
+#include "texture_ref.h"
 
 #include <cmath>
 #include <cstdint>
@@ -53,42 +54,19 @@ void bind(RefScene* s) {
 }
 
 // host textures for tex2D on texture objects (ids start at 1)
-struct HostTex {
-  std::vector<float4> texels;
-  int w = 0, h = 0;
-};
-std::map<unsigned long long, HostTex> g_tex;
+std::map<unsigned long long, orc::Texture> g_tex;
 
 }  // namespace
 
-// Linear filtering of a float4 texture with normalized coordinates and wrap
-// addressing (the texture descriptor of CreateCURTTexture,
-// src/cudaRTCommon.cu:418-448): x = frac(u) * W - 0.5, i = floor(x) and the
-// fractional weight a = frac(x) rounded to 8 fractional bits; the same in y;
-// the four texels (i, j), (i+1, j), (i, j+1), (i+1, j+1) wrap around and
-// are blended with (1-a)(1-b), a(1-b), (1-a)b, ab.
+// tex2D stand-in: the oracle's restatement of the linear, wrapped fetch
+// (texture_ref.h), so that the pin compares GetMaterialColors' own logic
+// (which texture, transparency times alpha, the emissive override).
 float4 gbref_tex2D_float4(cudaTextureObject_t obj, float u, float v) {
   auto it = g_tex.find(obj);
-  if (it == g_tex.end() || it->second.w <= 0 || it->second.h <= 0) return make_float4(0.f, 0.f, 0.f, 0.f);
-  const HostTex& t = it->second;
-  const float fu = u - std::floor(u);
-  const float fv = v - std::floor(v);
-  const float x = fu * (float)t.w - 0.5f;
-  const float y = fv * (float)t.h - 0.5f;
-  const float xf = std::floor(x), yf = std::floor(y);
-  const float a = std::nearbyint((x - xf) * 256.0f) / 256.0f;
-  const float b = std::nearbyint((y - yf) * 256.0f) / 256.0f;
-  auto wrap = [](long long i, int n) { long long r = i % n; return (int)(r < 0 ? r + n : r); };
-  const int i0 = wrap((long long)xf, t.w), i1 = wrap((long long)xf + 1, t.w);
-  const int j0 = wrap((long long)yf, t.h), j1 = wrap((long long)yf + 1, t.h);
-  const float4 t00 = t.texels[(size_t)j0 * t.w + i0], t10 = t.texels[(size_t)j0 * t.w + i1];
-  const float4 t01 = t.texels[(size_t)j1 * t.w + i0], t11 = t.texels[(size_t)j1 * t.w + i1];
-  const float w00 = (1.f - a) * (1.f - b), w10 = a * (1.f - b), w01 = (1.f - a) * b, w11 = a * b;
-  auto mix = [&](float c00, float c10, float c01, float c11) {
-    return ((w00 * c00 + w10 * c10) + w01 * c01) + w11 * c11;
-  };
-  return make_float4(mix(t00.x, t10.x, t01.x, t11.x), mix(t00.y, t10.y, t01.y, t11.y),
-                     mix(t00.z, t10.z, t01.z, t11.z), mix(t00.w, t10.w, t01.w, t11.w));
+  if (it == g_tex.end() || it->second.w == 0 || it->second.h == 0) return make_float4(0.f, 0.f, 0.f, 0.f);
+  float r[4];
+  orc::tex_bilinear<float>(it->second, u, v, r);
+  return make_float4(r[0], r[1], r[2], r[3]);
 }
 
 extern "C" {
@@ -213,11 +191,10 @@ void refpin_intersect_tri(const float* cases, uint32_t n, float eps, int32_t cul
 // Registers a W x H float4 texture (row-major, RGBA) under id (>= 1) for
 // the tex2D stand-in.
 void refpin_texture_set(uint64_t id, const float* rgba, int32_t w, int32_t h) {
-  HostTex t;
-  t.w = w;
-  t.h = h;
-  t.texels.resize((size_t)w * h);
-  std::memcpy(t.texels.data(), rgba, t.texels.size() * sizeof(float4));
+  orc::Texture t;
+  t.w = (uint32_t)w;
+  t.h = (uint32_t)h;
+  t.rgba.assign(rgba, rgba + (size_t)w * h * 4);
   g_tex[id] = std::move(t);
 }
 

@@ -90,6 +90,7 @@ def main(ref_root):
         t4["v1"] = t4["v0"] + 1
         t4["v2"] = t4["v0"] + 2
         m4 = np.zeros(1, layouts.MATERIAL)
+        m4[0] = layouts.material()  # untextured (texture ids -1)
         if oracle.Scene(v4, t4, m4).empty_children > 0:
             np.savez_compressed(os.path.join(HERE, "empty_children.npz"), vertices=v4, triangles=t4, materials=m4)
             break

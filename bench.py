@@ -1,18 +1,29 @@
-"""Benchmark of the GB300 streaming BDPT (plain "BDPTSC" mode).
+"""Benchmark of the GB300 streaming BDPT.  Prints one JSON line.
 
-Workload: the 1024x768 interior scene (20x10x30 room, 180 icospheres,
-57,614 triangles), eye and light depth caps 10, one progressive frame per
-step (786,432 camera paths), Philox seed 1234.  Prints one JSON line.
+Headline workload (``--workload hall``, the default): plain streaming BDPT
+("BDPTSC") on the procedural 332,180-triangle hall (40x8x40 room, 12x12
+pillars, 1200 displaced boxes, 4 lights) at 1280x720, eye and light depth
+caps 5 (the reference's compile-time caps), one progressive frame (921,600
+camera paths) per step, Philox seed 1234.  The same run also measures, on
+rank 0, the other benchmark configurations as secondary figures:
+
+* ``interior``: 1024x768, 20x10x30 room + 180 subdivision-3 icospheres
+  (230,414 triangles), constant environment 0.1, depth 10, 64 spp;
+* ``hall_adaptive``: the hall with the PLL adaptive allocator, 8 uniform
+  frames then 24 budgeted frames (32 spp mean), bilateral radius 4;
+* ``cornell``: the 36-triangle Cornell box, 256x256, depth 8, 16 spp;
+* batched serving (64 Poisson requests, saturated and below saturation).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
---impl reference times the reference algorithm's CPU implementation (the
-oracle restatement, multithreaded over the machine's host cores) on the same
-workload: the reference's own code is Windows/MSVC + CUDA 7.5 texture
-references and does not build here.
+--impl reference times the reference algorithm's CPU path on the machine's host
+cores: the oracle (a line-by-line restatement of the reference estimator,
+whose BVH builder and traversal equal the reference's own compiled code)
+over the same whole frames.  The reference's CUDA renderer is not run: it
+does not build with CUDA 13 without editing its sources, and its light pass
+writes past the end of its light-vertex buffer.
 """
 import argparse
-import ctypes
 import json
 import os
 import subprocess
@@ -27,22 +38,27 @@ sys.path.insert(0, ROOT)
 
 METRIC = "BDPT Mpaths/s"
 
-# name -> (scene generator, width, height, mode, depth caps, description)
+# name -> scene generator and kwargs, image size, renderer mode, depth cap, extra params,
+# frames that make one image, description
 WORKLOADS = {
-    "interior": ("interior", 1024, 768, 0, 10,
-                 "plain streaming BDPT, procedural interior 20x10x30 room + 180 icospheres (57,614 tris), "
-                 "1024x768, depth 10"),
-    "hall": ("hall", 1280, 720, 0, 5,
-             "plain streaming BDPT, procedural hall 40x8x40 + 144 pillars + 1200 boxes (332,180 tris), "
-             "1280x720, depth 5"),
-    "hall_adaptive": ("hall", 1280, 720, 1, 5,
-                      "adaptive BDPT + bilateral (radius 4), procedural hall (332,180 tris), 1280x720, depth 5, "
-                      "steady-state budgeted frames"),
-    "cornell": ("cornell", 256, 256, 0, 8,
-                "plain streaming BDPT, Cornell box (36 tris), 256x256, depth 8"),
+    "hall": dict(scene=("hall", {}), W=1280, H=720, mode=0, depth=5, params={}, image_frames=32,
+                 desc="plain streaming BDPT, procedural hall 40x8x40 + 144 pillars + 1200 boxes (332,180 tris), "
+                      "1280x720, depth 5"),
+    "interior": dict(scene=("interior", {"level": 3}), W=1024, H=768, mode=0, depth=10,
+                     params={"env": (0.1, 0.1, 0.1)}, image_frames=64,
+                     desc="plain streaming BDPT, procedural interior 20x10x30 room + 180 subdivision-3 icospheres "
+                          "(230,414 tris), constant environment 0.1, 1024x768, depth 10"),
+    "hall_adaptive": dict(scene=("hall", {}), W=1280, H=720, mode=1, depth=5,
+                          params={"filter_radius": 4, "warmup_frames": 8}, image_frames=32,
+                          desc="adaptive BDPT + bilateral (radius 4), procedural hall (332,180 tris), 1280x720, "
+                               "depth 5, 8 uniform + 24 budgeted frames"),
+    "cornell": dict(scene=("cornell", {}), W=256, H=256, mode=0, depth=8, params={}, image_frames=16,
+                    desc="plain streaming BDPT, Cornell box (36 tris), 256x256, depth 8, 16 spp"),
 }
-WL = WORKLOADS["interior"]
-WORKLOAD = WL[5]
+
+# static per-ray issue figures of the walk kernels, from single-kernel ncu captures
+ISSUE_PROFILES = {"hall": "profiles/k_walk_hall_640x360.md", "interior": "profiles/k_walk_k_tail_interior_512x384.md"}
+SMS, SCHEDULERS = 152, 4
 
 
 def dist_env():
@@ -80,6 +96,7 @@ class ClockSampler:
                  "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            time.sleep(0.3)  # the first sample lands before the timed work starts
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -115,292 +132,67 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def scene_and_camera():
+def scene_and_camera(wl):
     from cudapt_gb300 import scenes
-    return getattr(scenes, WL[0])()
+    name, kw = wl["scene"]
+    return getattr(scenes, name)(**kw)
 
 
-def params_for(gb_or_layouts, **kw):
-    extra = dict(filter_radius=4) if WL[3] == 1 else {}
+def params_for(mod, wl, **kw):
+    extra = dict(wl["params"])
     extra.update(kw)
-    return gb_or_layouts.default_params(eye_depth_max=WL[4], light_depth_max=WL[4], **extra)
+    return mod.default_params(eye_depth_max=wl["depth"], light_depth_max=wl["depth"], **extra)
 
 
-W, H = WL[1], WL[2]
-
-
-def run_cpu_sample(threads, rows, frames=1, seed=1234, bands=4):
-    """Oracle (CPU restatement of the reference estimator) on `rows` full-width
-    rows of the same workload, split into `bands` bands spread evenly over the
-    image so that the sample's cost per path matches the whole frame's;
-    returns (paths, seconds, build_seconds)."""
+def run_cpu_frames(wl, threads, budget_s, max_frames, seed=1234, scene=None):
+    """The oracle (CPU restatement of the reference estimator, its BVH builder
+    and traversal equal to the reference's compiled code) on whole frames of
+    the workload: frames until `budget_s` of render time or `max_frames`.
+    Returns (paths, render seconds, frames, build seconds)."""
     import oracle
     from cudapt_gb300 import layouts
-    (v, t, m), cam = scene_and_camera()
-    sc = oracle.Scene(v, t, m)
-    p = params_for(layouts, seed=seed)
-    bands = max(1, min(bands, rows))
-    per = [rows // bands + (1 if b < rows % bands else 0) for b in range(bands)]
-    dt = 0.0
-    for b, rb in enumerate(per):
-        y0 = (H - rb) * b // max(bands - 1, 1)
-        r = oracle.Renderer(W, rb, 0, p, threads=threads)
-        r.set_window(0, y0, W, H)
+    (v, t, m), cam = scene_and_camera(wl)
+    sc = scene if scene is not None else oracle.Scene(v, t, m)
+    p = params_for(layouts, wl, seed=seed)
+    r = oracle.Renderer(wl["W"], wl["H"], wl["mode"], p, threads=threads)
+    paths, secs, frames = 0, 0.0, 0
+    while frames < max_frames and (frames == 0 or secs < budget_s):
         t0 = time.perf_counter()
-        r.render(sc, cam, frames)
-        dt += time.perf_counter() - t0
-    return W * rows * frames, dt, sc.build_seconds
+        r.render(sc, cam, 1)
+        secs += time.perf_counter() - t0
+        paths += r.stats()["paths"]
+        frames += 1
+    return paths, secs, frames, sc.build_seconds, sc
 
 
-def bench_reference(args):
+def bench_reference(args, wl):
+    """The reference arm: the CPU path on the host cores, whole frames of the
+    same workload, one frame per step."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    import oracle
+    oracle.build()
     threads = os.cpu_count() or 1
-    # bounded sample per step: a quarter of the frame's rows in 4 bands
-    rows = int(os.environ.get("GBPT_REF_ROWS", str(H // 4)))
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        run_cpu_sample(threads, 4)
-    paths = secs = 0.0
-    for _ in range(args.steps):
-        p, dt, build_s = run_cpu_sample(threads, rows)
-        paths += p
-        secs += dt
-    v = paths / secs / 1e6
+    (v, t, m), _ = scene_and_camera(wl)
+    sc = oracle.Scene(v, t, m)
+    run_cpu_frames(wl, threads, 0.0, 1, scene=sc)  # warm-up: one frame (page-in, thread start)
+    paths, secs, frames, build_s, _ = run_cpu_frames(wl, threads, 1e9, args.steps, scene=sc)
+    v_ = paths / secs / 1e6
+    sample = (f"{frames} whole {wl['W']}x{wl['H']} frames (one per step) of the same workload, oracle FP32 "
+              f"estimator on {threads} host threads ({build_s:.2f} s BVH build, reported separately)")
     line = {
-        "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Mpaths/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 2),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "width": W, "height": H, "paths_per_step": W * rows,
-                   "sample": f"{W}x{rows} rows per step in 4 bands spread over the frame"},
-        "cpu_baseline": {"value": round(v, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
-                         "sample": f"{W}x{rows} rows (4 bands) x {args.steps} steps, oracle FP32 estimator + restated BVH build "
-                                   f"({build_s:.2f} s build)"},
-        "e2e": {"value": round(v, 4), "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
-
-
-def bench_gpu(args):
-    rank, world, local = dist_env()
-    import cudapt_gb300 as gb
-    from cudapt_gb300 import build as gbuild
-    gbuild.build()
-    if world > 1:
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
-    if not gb.device_available():
-        raise SystemExit("bench: no usable CUDA device")
-    (v, t, m), cam = scene_and_camera()
-    scene = gb.RTScene(v, t, m).build_bvh()
-    build_s = scene.build_seconds
-    if args.traversal == "wide":
-        scene.set_traversal("wide")
-    params = params_for(gb)
-    np_ = W * H
-    r = gb.RTRenderer(W, H, WL[3], params)
-
-    flush = FlushBuffer()
-    # warm-up (the adaptive workload first runs its uniform frames, so that
-    # every timed step is a budgeted + filtered frame)
-    warm = max(args.warmup, 0) + (int(params["warmup_frames"]) if WL[3] == 1 else 0)
-    for _ in range(warm):
-        r.render_frames(scene, cam, 1, stats=True)
-    # timed: one frame per step, L2 flushed (256 MB device memset) before each
-    ms = []
-    phases = {"ms_trace": 0.0, "ms_shade": 0.0, "ms_light": 0.0, "ms_filter": 0.0, "ms_adapt": 0.0,
-              "ms_total": 0.0}
-    rays = 0
-    paths = 0
-    launches = 0
-    with ClockSampler(0) as clk:
-        for _ in range(args.steps):
-            flush()
-            st = r.render_frames(scene, cam, 1, stats=True)
-            ms.append(st["ms_total"])
-            rays += st["rays"]
-            paths += st["paths"]
-            launches += st["launches"]
-            for k in phases:
-                phases[k] += st[k]
-    total_ms = float(np.sum(ms))
-    value = paths / (total_ms / 1e3) / 1e6
-
-    # the same frames with the wide traversal (opt-in; same hits except surfaces closer together
-    # than the reference's origin push), timed the same way on a second renderer
-    wide = None
-    if args.traversal == "reference" and not args.no_wide:
-        scene.set_traversal("wide")
-        rw = gb.RTRenderer(W, H, WL[3], params)
-        for _ in range(warm):
-            rw.render_frames(scene, cam, 1, stats=True)
-        wms, wpaths = [], 0
-        for _ in range(args.steps):
-            flush()
-            st = rw.render_frames(scene, cam, 1, stats=True)
-            wms.append(st["ms_total"])
-            wpaths += st["paths"]
-        wv = wpaths / (float(np.sum(wms)) / 1e3) / 1e6
-        wide = {"value": round(wv * world, 3), "ms_per_step": round(float(np.mean(wms)), 4),
-                "tree": "binary tree collapsed to 4 children per node, nearest child first",
-                "hits": "the reference's closest hit except where two surfaces lie within its 1e-4 origin push "
-                        "of each other (tests/test_wide.py; 0.8% of random rays in the Cornell box, whose "
-                        "blocks stand on the floor)"}
-        rw.close()
-        scene.set_traversal("reference")
-
-    # e2e through the public call with a host result buffer (D2H of the image each step)
-    out = np.zeros(np_ * 3, np.float32)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        r.render(scene, cam, stats=False)
-    e2e_s = time.perf_counter() - t0
-    e2e = paths / e2e_s / 1e6
-
-    # work counters for the roofline (separate, untimed frame)
-    r.set_counting(True)
-    cst = r.render_frames(scene, cam, 1, stats=True)
-    r.set_counting(False)
-    # bytes per visited node: 32 B bounds + 8 B child words (reference order); 112 B per
-    # wide node (4 boxes + 4 child codes); 48 B per triangle test
-    node_bytes = 112 if args.traversal == "wide" else 40
-    trace_bytes = node_bytes * (cst["nodes"] + cst["shadow_nodes"]) + 48 * (cst["tris"] + cst["shadow_tris"])
-    # the counting frame runs the counting variants of the walks (slower): its work
-    # counts, over the timed frames' mean walk time
-    trace_ms = phases["ms_trace"] / max(args.steps, 1)
-    achieved = trace_bytes / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else None
-    peak, peak_kind = load_peaks()
-
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        rows = int(os.environ.get("GBPT_CPU_ROWS", str(H)))  # the whole frame
-        p, dt, bs = run_cpu_sample(threads, rows)
-        cpu = {"value": round(p / dt / 1e6, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
-               "sample": f"{W}x{rows} rows (4 bands spread over the frame) of one uniform frame, oracle FP32 estimator "
-                         f"({bs:.2f} s restated BVH build)"}
-
-    serving = None
-    if rank == 0 and not args.no_serving:
-        serving = serving_run(gb)
-
-    D = int(params["eye_depth_max"])
-    traffic = profiled_traffic(args.workload)
-    line = {
-        "metric": METRIC, "value": round(value * world, 3), "unit": "Mpaths/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
+        "impl": "reference", "metric": METRIC, "value": round(v_, 4), "unit": "Mpaths/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / max(frames, 1), 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (procedural scene, seeded)",
-        "config": {"workload": WORKLOAD, "width": W, "height": H, "paths_per_step": np_,
-                   "eye_depth_max": D, "light_depth_max": D, "tris": int(len(t)),
-                   "l2": "flushed before every timed step (256 MB device memset)",
-                   "bvh_build_s": round(build_s, 4), "rays_per_s": round(rays / (total_ms / 1e3), 1),
-                   "traversal": args.traversal,
-                   "phase_ms_per_step": {k: round(v_ / args.steps, 4) for k, v_ in phases.items()},
-                   "parallelism": "replicas" if world > 1 else "single"},
-        "e2e": {"value": round(e2e * world, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": 40,
-                "d2h_bytes_per_step": np_ * 12},
-        "roofline": {"bound": "hbm", "kernel": "k_walk + k_tail (closest-hit + shadow BVH walks of one frame)",
-                     "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4) if achieved else None, "peak_kind": peak_kind,
-                     "traffic": traffic,
-                     "algorithmic_bytes_per_frame": int(trace_bytes),
-                     # the tree and triangles are L2-resident: the L2 side of the same walks
-                     "l2": l2_side(args.workload, trace_ms)},
-        "filter_roofline": filter_roofline(phases, args.steps, np_, peak) if WL[3] == 1 else None,
-        "wide_traversal": wide,
-        "learned_sampler": learned_sampler_summary(),
-        "serving": serving,
-        "cpu_baseline": cpu,
-        "clocks": clk.summary(),
-        "gpu_launches": launches,
+        "config": {"workload": wl["desc"], "width": wl["W"], "height": wl["H"], "paths_per_step": wl["W"] * wl["H"],
+                   "sample": "whole frames, one per step", "bvh_build_s": round(build_s, 3)},
+        "cpu_baseline": {"value": round(v_, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(v_, 4), "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-
-
-def serving_run(gb, n=64, rate=200.0, seed=0, workers=4):
-    """The batched-serving configuration: n requests arriving as a Poisson
-    process (rate per second), each a scene of the three plain benchmark
-    scenes, a resolution of {128^2, 256^2, 512^2, 1024x768}, {4, 16, 64}
-    spp and depth cap {6, 8, 10}; BVHs resident on the device, `workers`
-    requests in flight (cudapt_gb300.serving)."""
-    from cudapt_gb300 import scenes, serving
-    objs, cams = {}, {}
-    for name in ("cornell", "interior", "hall"):
-        (v, t, m), cam = getattr(scenes, name)()
-        objs[name] = gb.RTScene(v, t, m).build_bvh()
-        cams[name] = cam
-    wl = serving.poisson_workload(n, rate, seed)
-    summary, st = serving.run_poisson(gb, wl, objs, cams, workers=workers)
-    summary["config"] = (f"{n} requests, Poisson {rate:g}/s (seed {seed}), scenes cornell/interior/hall, "
-                         "resolution in {128^2, 256^2, 512^2, 1024x768}, spp in {4, 16, 64}, depth in {6, 8, 10}, "
-                         "plain BDPT, image copied to page-locked host memory per request")
-    summary["unit"] = "Mpaths/s (all requests' camera paths / wall time from first arrival to last completion)"
-    for s_ in objs.values():
-        s_.close()
-    return summary
-
-
-def l2_side(workload, trace_ms):
-    """L2 bytes of one frame's walks (32-byte sectors, profiles/walk_traffic_<workload>.txt)
-    over this run's walk time, with the walk kernel's L2 throughput in percent of
-    peak as ncu reports it (profiles/k_walk_k_tail_interior_1024x768.md)."""
-    b = profiled_traffic(workload, "l2_bytes_per_frame")
-    if b is None or not trace_ms:
-        return None
-    return {"bytes_per_frame": b, "achieved_GBs": round(b / (trace_ms / 1e3) / 1e9, 1),
-            "throughput_pct_of_peak_ncu": [21.5, 16.8],
-            "note": "L2 serves the walks' node and triangle fetches that miss L1 (74-75% L1 hit rate); "
-                    "L2 throughput 17-22% of peak: latency-bound, not bandwidth-bound"}
-
-
-def filter_roofline(phases, steps, np_, peak):
-    """Bilateral filter of a budgeted frame against its compulsory traffic: the colour,
-    position and normal planes read (12 B per pixel each) and 12 B per pixel written."""
-    ms = phases["ms_filter"] / steps
-    if ms <= 0:
-        return None
-    planes = 3
-    compulsory = (planes * 12 + 12) * np_
-    radius = 4
-    gbs = compulsory / (ms / 1e3) / 1e9
-    return {"kernel": "k_bilateral_tile", "bound": "hbm", "ms_per_frame": round(ms, 4),
-            "compulsory_bytes": compulsory, "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(gbs / peak, 4),
-            "taps_per_pixel": (2 * radius + 1) ** 2,
-            "algorithmic_bytes_naive": (2 * radius + 1) ** 2 * planes * 12 * np_}
-
-
-def learned_sampler_summary():
-    """Equal-time RMSE of the learned allocator over the plain PLL allocator (held-out hall
-    scenes), from the committed report of tests/experiments/learned_sampler.py."""
-    p = os.path.join(ROOT, "profiles", "learned_sampler_hall_320x180.md")
-    if not os.path.exists(p):
-        return None
-    out = {"report": "profiles/learned_sampler_hall_320x180.md", "scenes": "hall seeds 21-25, 320x180",
-           "equal_time_s": [0.25, 0.5, 1.0]}
-    with open(p) as f:
-        for ln in f:
-            parts = ln.split()
-            if len(parts) == 2 and parts[0].startswith("learned_over_plain_rmse_"):
-                out[parts[0]] = float(parts[1])
-    return out
-
-
-def profiled_traffic(workload, key="traffic_bytes_per_frame"):
-    """A figure of the BVH-walk launches of one frame from the committed ncu
-    summary of this workload (profiles/walk_traffic_<workload>.txt, line
-    ``<key> <n>``): DRAM bytes (read + write) by default, ``l2_bytes_per_frame``
-    for the L2's; None when no capture exists."""
-    p = os.path.join(ROOT, "profiles", f"walk_traffic_{workload}.txt")
-    if not os.path.exists(p):
-        return None
-    with open(p) as f:
-        for ln in f:
-            parts = ln.split()
-            if len(parts) == 2 and parts[0] == key:
-                return int(parts[1])
-    return None
+    print(json.dumps(line), flush=True)
 
 
 class FlushBuffer:
@@ -416,26 +208,300 @@ class FlushBuffer:
         self.torch.cuda.synchronize()
 
 
+PHASES = ("ms_trace", "ms_shade", "ms_light", "ms_filter", "ms_adapt", "ms_total")
+
+
+def timed_frames(r, scene, cam, steps, flush):
+    """`steps` frames, one per step, L2 flushed before each; device times from
+    the library's CUDA events on the renderer's stream."""
+    ph = {k: 0.0 for k in PHASES}
+    rays = paths = launches = 0
+    for _ in range(steps):
+        flush()
+        st = r.render_frames(scene, cam, 1, stats=True)
+        rays += st["rays"]
+        paths += st["paths"]
+        launches += st["launches"]
+        for k in PHASES:
+            ph[k] += st[k]
+    return ph, rays, paths, launches
+
+
+def walk_bytes(r, scene, cam, traversal="reference"):
+    """Algorithmic bytes of one frame's BVH walks, counted by the kernels in an
+    untimed frame: 40 B per node visit (32 B bounds + 8 B child words; 112 B
+    per wide node) and 48 B per triangle test, closest-hit and any-hit walks."""
+    r.set_counting(True)
+    cst = r.render_frames(scene, cam, 1, stats=True)
+    r.set_counting(False)
+    node_bytes = 112 if traversal == "wide" else 40
+    return (node_bytes * (cst["nodes"] + cst["shadow_nodes"]) + 48 * (cst["tris"] + cst["shadow_tris"]), cst)
+
+
+def read_profile(path):
+    """``key value`` lines of a committed profile summary (figures taken from an
+    ncu capture whose command the file names)."""
+    p = os.path.join(ROOT, path)
+    out = {}
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for ln in f:
+            parts = ln.strip().strip("`").split()
+            if len(parts) == 2:
+                try:
+                    out[parts[0]] = float(parts[1])
+                except ValueError:
+                    pass
+    return out
+
+
+def issue_side(name, trace_ms, rays_per_frame, sm_mhz):
+    """Issue-slot use of the walk kernels: warp instructions per ray from a
+    single-kernel ncu capture (static, the file is named), times this run's
+    rays, over 152 SMs x 4 schedulers x the sampled SM clock x this run's
+    walk time; lanes active per instruction from the same capture."""
+    src = ISSUE_PROFILES.get(name)
+    prof = read_profile(src) if src else None
+    if not prof or "warp_inst_per_ray" not in prof or not trace_ms or not sm_mhz:
+        return None
+    inst = prof["warp_inst_per_ray"] * rays_per_frame
+    slots = SMS * SCHEDULERS * sm_mhz * 1e6 * trace_ms / 1e3
+    return {"frac": round(inst / slots, 4), "lanes_active_per_inst": prof.get("lanes_active_per_inst"),
+            "lane_frac": round(inst / slots * prof.get("lanes_active_per_inst", 0.0) / 32.0, 4),
+            "warp_inst_per_ray": prof["warp_inst_per_ray"],
+            "static_source": src + " (instructions per ray and lanes per instruction; the rest measured in this run)"}
+
+
+def measure_workload(gb, name, steps, warmup, flush, peak):
+    """One benchmark configuration on its own renderer: `steps` timed frames
+    (budgeted frames for the adaptive one, after its uniform frames), the
+    whole image (all its frames) timed once, and the walks' work rate."""
+    wl = WORKLOADS[name]
+    (v, t, m), cam = scene_and_camera(wl)
+    scene = gb.RTScene(v, t, m).build_bvh()
+    params = params_for(gb, wl)
+    r = gb.RTRenderer(wl["W"], wl["H"], wl["mode"], params)
+    warm = warmup + (int(params["warmup_frames"]) if wl["mode"] == 1 else 0)
+    for _ in range(warm):
+        r.render_frames(scene, cam, 1, stats=True)
+    ph, rays, paths, launches = timed_frames(r, scene, cam, steps, flush)
+    tb, _ = walk_bytes(r, scene, cam)
+    # the whole image: its frames from a reset, one call each (uniform + budgeted for the adaptive one),
+    # device time and camera paths summed over the frames
+    r.reset()
+    flush()
+    img_ms, img_paths = 0.0, 0
+    for _ in range(wl["image_frames"]):
+        st = r.render_frames(scene, cam, 1, stats=True)
+        img_ms += st["ms_total"]
+        img_paths += st["paths"]
+    trace_ms = ph["ms_trace"] / steps
+    out = {"workload": wl["desc"], "tris": int(len(t)), "width": wl["W"], "height": wl["H"],
+           "value": round(paths / (ph["ms_total"] / 1e3) / 1e6, 3), "unit": "Mpaths/s",
+           "ms_per_frame": round(ph["ms_total"] / steps, 4), "frames_timed": steps,
+           "rays_per_s": round(rays / (ph["ms_total"] / 1e3), 1),
+           "phase_ms_per_frame": {k: round(x / steps, 4) for k, x in ph.items()},
+           "image": {"frames": wl["image_frames"], "ms": round(img_ms, 3), "paths": int(img_paths),
+                     "mpaths_per_s": round(img_paths / (img_ms / 1e3) / 1e6, 3)},
+           "walk_work_rate": {"bytes_per_frame": int(tb), "achieved_GBs": round(tb / (trace_ms / 1e3) / 1e9, 1),
+                              "frac_of_hbm": round(tb / (trace_ms / 1e3) / 1e9 / peak, 4)} if trace_ms else None}
+    if name == "hall_adaptive":
+        out["filter"] = filter_roofline(ph, steps, wl["W"] * wl["H"], peak, int(params["filter_radius"]))
+    r.close()
+    scene.close()
+    return out
+
+
+def filter_roofline(phases, steps, np_, peak, radius):
+    """Bilateral filter of a budgeted frame against its compulsory traffic: the colour,
+    position and normal planes read (12 B per pixel each) and 12 B per pixel written."""
+    ms = phases["ms_filter"] / steps
+    if ms <= 0:
+        return None
+    planes = 3
+    compulsory = (planes * 12 + 12) * np_
+    gbs = compulsory / (ms / 1e3) / 1e9
+    return {"kernel": "k_bilateral_tile", "bound": "hbm", "ms_per_frame": round(ms, 4),
+            "compulsory_bytes": compulsory, "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(gbs / peak, 4), "taps_per_pixel": (2 * radius + 1) ** 2,
+            "algorithmic_bytes_naive": (2 * radius + 1) ** 2 * planes * 12 * np_}
+
+
+def bench_gpu(args, wl):
+    rank, world, local = dist_env()
+    import cudapt_gb300 as gb
+    from cudapt_gb300 import build as gbuild
+    gbuild.build()
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    if not gb.device_available():
+        raise SystemExit("bench: no usable CUDA device")
+    W, H = wl["W"], wl["H"]
+    (v, t, m), cam = scene_and_camera(wl)
+    scene = gb.RTScene(v, t, m).build_bvh()
+    build_s = scene.build_seconds
+    if args.traversal == "wide":
+        scene.set_traversal("wide")
+    params = params_for(gb, wl)
+    np_ = W * H
+    r = gb.RTRenderer(W, H, wl["mode"], params)
+    peak, peak_kind = load_peaks()
+
+    flush = FlushBuffer()
+    # warm-up (the adaptive workload first runs its uniform frames, so that
+    # every timed step is a budgeted + filtered frame)
+    warm = max(args.warmup, 0) + (int(params["warmup_frames"]) if wl["mode"] == 1 else 0)
+    for _ in range(warm):
+        r.render_frames(scene, cam, 1, stats=True)
+    with ClockSampler(0) as clk:
+        phases, rays, paths, launches = timed_frames(r, scene, cam, args.steps, flush)
+    clocks = clk.summary()
+    total_ms = phases["ms_total"]
+    value = paths / (total_ms / 1e3) / 1e6
+
+    # e2e through the public call with a host result buffer (D2H of the image each step)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r.render(scene, cam, stats=False)
+    e2e_s = time.perf_counter() - t0
+    e2e = paths / e2e_s / 1e6
+
+    trace_bytes, cst = walk_bytes(r, scene, cam, args.traversal)
+    trace_ms = phases["ms_trace"] / max(args.steps, 1)
+    achieved = trace_bytes / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else None
+    rays_per_frame = rays / max(args.steps, 1)
+    prof = read_profile(f"profiles/k_walk_{args.workload}_traffic.md") or {}
+
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        # the same frames with the opt-in wide traversal, timed the same way on a second renderer
+        if args.traversal == "reference":
+            scene.set_traversal("wide")
+            rw = gb.RTRenderer(W, H, wl["mode"], params)
+            for _ in range(warm):
+                rw.render_frames(scene, cam, 1, stats=True)
+            wph, _, wpaths, _ = timed_frames(rw, scene, cam, args.steps, flush)
+            extras["wide_traversal"] = {
+                "value": round(wpaths / (wph["ms_total"] / 1e3) / 1e6, 3),
+                "ms_per_step": round(wph["ms_total"] / args.steps, 4),
+                "tree": "binary tree collapsed to 4 children per node, nearest child first (opt-in)",
+                "hits": "the reference's closest hit except where two surfaces lie within its 1e-4 origin push of "
+                        "each other (tests/test_wide.py)"}
+            rw.close()
+            scene.set_traversal("reference")
+        others = {}
+        for name in WORKLOADS:
+            if name != args.workload:
+                steps = 24 if name == "hall_adaptive" else max(4, min(args.steps, 10))
+                others[name] = measure_workload(gb, name, steps, 2, flush, peak)
+        extras["other_configs"] = others
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        p_, dt, frames, bs, _ = run_cpu_frames(wl, threads, 10.0, 40)
+        cpu = {"value": round(p_ / dt / 1e6, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
+               "sample": f"{frames} whole {W}x{H} frames of the same workload (about 10 s), oracle FP32 estimator "
+                         f"({bs:.2f} s BVH build, reported separately)"}
+
+    if rank == 0 and not args.no_serving:
+        extras["serving"] = serving_run(gb)
+
+    line = {
+        "metric": METRIC, "value": round(value * world, 3), "unit": "Mpaths/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (procedural scene, seeded)",
+        "config": {"workload": wl["desc"], "width": W, "height": H, "paths_per_step": np_,
+                   "eye_depth_max": wl["depth"], "light_depth_max": wl["depth"], "tris": int(len(t)),
+                   "l2": "flushed before every timed step (256 MB device memset)",
+                   "bvh_build_s": round(build_s, 4), "rays_per_s": round(rays / (total_ms / 1e3), 1),
+                   "traversal": args.traversal,
+                   "phase_ms_per_step": {k: round(v_ / args.steps, 4) for k, v_ in phases.items()},
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": round(e2e * world, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": 40,
+                "d2h_bytes_per_step": np_ * 12},
+        "roofline": {
+            "bound": "hbm", "kernel": "k_walk + k_tail (closest-hit + shadow BVH walks of one frame)",
+            "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4) if achieved else None, "peak_kind": peak_kind,
+            "note": "work rate: algorithmic walk bytes (40 B per node visit, 48 B per triangle test, counted by the "
+                    "kernels in an untimed frame of this run) over this run's walk time; the tree is L2-resident, "
+                    "so DRAM carries a small part of these bytes and the issue side below is the real limit",
+            "algorithmic_bytes_per_frame": int(trace_bytes),
+            "traffic": int(prof["dram_bytes_per_frame"]) if "dram_bytes_per_frame" in prof else None,
+            "traffic_source": (f"profiles/k_walk_{args.workload}_traffic.md (static: DRAM bytes of one frame's walk "
+                               f"launches from an ncu capture)") if "dram_bytes_per_frame" in prof else None,
+            "issue": issue_side(args.workload, trace_ms, rays_per_frame, clocks.get("sm_mhz")),
+        },
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": launches,
+        "extra_keys": sorted(extras),
+    }
+    line.update(extras)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    r.close()
+
+
+def serving_run(gb, n=64, rate=200.0, seed=0, workers=4):
+    """The batched-serving configuration: n requests arriving as a Poisson
+    process, each a scene of the three plain benchmark scenes, a resolution of
+    {128^2, 256^2, 512^2, 1024x768}, {4, 16, 64} spp and depth cap {6, 8, 10};
+    BVHs resident on the device, `workers` requests in flight
+    (cudapt_gb300.serving).  Run at the configuration's rate (about 10x the
+    GPU's capacity: latency is queueing) and again at 0.6x the capacity that
+    run measured (latency is service time)."""
+    from cudapt_gb300 import scenes, serving
+    objs, cams = {}, {}
+    for name in ("cornell", "interior", "hall"):
+        (v, t, m), cam = getattr(scenes, name)()
+        objs[name] = gb.RTScene(v, t, m).build_bvh()
+        cams[name] = cam
+    wl = serving.poisson_workload(n, rate, seed)
+    summary, st = serving.run_poisson(gb, wl, objs, cams, workers=workers)
+    summary["rate_per_s"] = rate
+    cap = summary["requests"] / summary["wall_s"]
+    low_rate = round(0.6 * cap, 2)
+    low, _ = serving.run_poisson(gb, serving.poisson_workload(n, low_rate, seed), objs, cams, workers=workers)
+    low["rate_per_s"] = low_rate
+    out = {"saturated": summary, "below_saturation": low,
+           "capacity_requests_per_s": round(cap, 2),
+           "config": (f"{n} requests, Poisson {rate:g}/s and 0.6x measured capacity (seed {seed}), scenes "
+                      "cornell/interior/hall, resolution in {128^2, 256^2, 512^2, 1024x768}, spp in {4, 16, 64}, "
+                      "depth in {6, 8, 10}, plain BDPT, image copied to page-locked host memory per request"),
+           "unit": "Mpaths/s (all requests' camera paths / wall time from first arrival to last completion)"}
+    for s_ in objs.values():
+        s_.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbpt", choices=["gbpt", "reference"])
-    ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="interior", choices=sorted(WORKLOADS))
-    ap.add_argument("--no-wide", action="store_true", help="skip the extra wide-traversal timing")
-    ap.add_argument("--no-serving", action="store_true", help="skip the batched-serving run")
+    ap.add_argument("--workload", default="hall", choices=sorted(WORKLOADS))
+    ap.add_argument("--size", default=None, help="WxH override (profiling captures of a smaller frame)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-extras", action="store_true", help="skip the wide walk and the other configurations")
+    ap.add_argument("--no-serving", action="store_true", help="skip the batched-serving runs")
     ap.add_argument("--traversal", default="reference", choices=["reference", "wide"],
                     help="BVH walk order: the reference's (bit-exact, default) or the collapsed 4-wide tree")
     args = ap.parse_args()
-    global WL, WORKLOAD, W, H
-    WL = WORKLOADS[args.workload]
-    WORKLOAD, W, H = WL[5], WL[1], WL[2]
+    wl = dict(WORKLOADS[args.workload])
+    if args.size:
+        w, h = (int(x) for x in args.size.lower().split("x"))
+        wl.update(W=w, H=h, desc=wl["desc"] + f" (frame size {w}x{h})")
+    if args.warmup < 3:
+        print("bench: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
-        bench_reference(args)
+        bench_reference(args, wl)
     else:
-        bench_gpu(args)
+        bench_gpu(args, wl)
 
 
 if __name__ == "__main__":

@@ -371,7 +371,8 @@ def bench_gpu(args, wl):
     trace_ms = phases["ms_trace"] / max(args.steps, 1)
     achieved = trace_bytes / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else None
     rays_per_frame = rays / max(args.steps, 1)
-    prof = read_profile(f"profiles/k_walk_{args.workload}_traffic.md") or {}
+    prof_src = ISSUE_PROFILES.get(args.workload)
+    prof = (read_profile(prof_src) or {}) if prof_src else {}
 
     extras = {}
     if rank == 0 and not args.no_extras:
@@ -430,9 +431,11 @@ def bench_gpu(args, wl):
                     "kernels in an untimed frame of this run) over this run's walk time; the tree is L2-resident, "
                     "so DRAM carries a small part of these bytes and the issue side below is the real limit",
             "algorithmic_bytes_per_frame": int(trace_bytes),
-            "traffic": int(prof["dram_bytes_per_frame"]) if "dram_bytes_per_frame" in prof else None,
-            "traffic_source": (f"profiles/k_walk_{args.workload}_traffic.md (static: DRAM bytes of one frame's walk "
-                               f"launches from an ncu capture)") if "dram_bytes_per_frame" in prof else None,
+            "traffic": int(prof["dram_bytes_per_path"] * np_) if "dram_bytes_per_path" in prof else None,
+            "traffic_source": (f"{prof_src} (static: DRAM bytes per camera path of one frame's walk launches in an "
+                               f"ncu capture of a smaller frame of the same scene, times this frame's paths)")
+            if "dram_bytes_per_path" in prof else None,
+            "l2_bytes_per_frame": int(prof["l2_bytes_per_path"] * np_) if "l2_bytes_per_path" in prof else None,
             "issue": issue_side(args.workload, trace_ms, rays_per_frame, clocks.get("sm_mhz")),
         },
         "cpu_baseline": cpu,

@@ -310,6 +310,12 @@ struct gbpt_renderer {
   // current frames do not read; tag = (epoch, frame) the cache was made for
   cudaStream_t stLight = nullptr;
   cudaEvent_t evMain = nullptr, evLight[2] = {nullptr, nullptr};
+  // bands: a frame's camera paths split into bands, one wavefront each on its
+  // own stream, forked from and joined to the work stream by events, so that
+  // one band's last long walks overlap the others' work
+  cudaStream_t stBand[kMaxBands] = {};
+  cudaEvent_t evFork = nullptr, evJoin[kMaxBands] = {};
+  uint32_t lastBands = 1;
   // frames issued as CUDA graphs (plain and PTSC modes): executable graphs
   // without / with an inline light pass
   bool graphs = false, graphWarm = false;
@@ -380,8 +386,15 @@ struct gbpt_renderer {
     for (auto e : evPool) cudaEventDestroy(e);
     for (cudaGraphExec_t& x : gexec)
       if (x) cudaGraphExecDestroy(x);
-    for (cudaEvent_t e : {evMain, evLight[0], evLight[1]})
+    for (cudaEvent_t e : {evMain, evLight[0], evLight[1], evFork})
       if (e) cudaEventDestroy(e);
+    for (uint32_t b = 0; b < kMaxBands; b++) {
+      if (evJoin[b]) cudaEventDestroy(evJoin[b]);
+      if (stBand[b]) {
+        cudaStreamSynchronize(stBand[b]);
+        cudaStreamDestroy(stBand[b]);
+      }
+    }
     if (stLight) cudaStreamDestroy(stLight);
     if (st && !userStream) cudaStreamDestroy(st);
     if (ownSt && ownSt != st) cudaStreamDestroy(ownSt);
@@ -402,7 +415,40 @@ gbpt_status check_params(const gbpt_params* p) {
   if (p->pt_depth_max < 1 || p->pt_depth_max > 64) return fail(GBPT_ERR_INVALID_ARG, "pt_depth_max must be 1..64");
   if (p->walk_refill > 32) return fail(GBPT_ERR_INVALID_ARG, "walk_refill must be 0..32");
   if (p->tail_from < -1) return fail(GBPT_ERR_INVALID_ARG, "tail_from must be >= -1");
+  if (p->bands > kMaxBands) return fail(GBPT_ERR_INVALID_ARG, "bands must be 0..8");
   return GBPT_OK;
+}
+
+// Bands of a frame: `requested` when set, else 2 from 512K camera paths.
+// Measured on GB300 (Mpaths/s, 1 / 2 / 3 / 4 bands): hall 1280x720 175.6 /
+// 180.9 / 176.4 / 165.3, interior 1024x768 154.7 / 157.4 / 144.8 / 137.1,
+// Cornell 256x256 206.3 / 188.6 (1 / 2).  A band's persistent walk holds its
+// SMs until its queue drains, so the bands of one frame stay nearly in step.
+uint32_t bands_for(uint32_t requested, size_t paths) {
+  if (requested) return std::min<uint32_t>(requested, kMaxBands);
+  return paths >= (1u << 19) ? 2u : 1u;
+}
+
+// The buffers of band b of k: pixels [b*np/k, (b+1)*np/k); the wave, hit and
+// connection-queue arrays start at the band's first pixel, the counters are
+// the band's own.
+RenderBuffers band_buffers(const RenderBuffers& rb, uint32_t b, uint32_t k, size_t np) {
+  RenderBuffers x = rb;
+  const size_t p0 = np * b / k, p1 = np * (b + 1) / k;
+  x.base = (uint32_t)p0;
+  x.count = (uint32_t)(p1 - p0);
+  for (int w = 0; w < 2; w++) {
+    x.wave[w].o += p0;
+    x.wave[w].d += p0;
+    x.wave[w].thr += p0;
+    x.wave[w].smp += p0;
+  }
+  x.hit += p0;
+  x.sh[0] += 3 * p0;
+  x.sh[1] += 3 * p0;
+  x.ctr = rb.ctr + b;
+  x.lctr = rb.ctr;
+  return x;
 }
 
 }  // namespace
@@ -442,8 +488,11 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   CK(dalloc(&r->rb.slotSmp, cap));
   CK(dalloc(&r->rb.cache[0], (size_t)cacheCap * 6));
   CK(dalloc(&r->rb.cache[1], (size_t)cacheCap * 6));
-  CK(dalloc(&r->rb.ctr, 1));
-  CK(cudaMemsetAsync(r->rb.ctr, 0, sizeof(DevCounters), r->st));
+  CK(dalloc(&r->rb.ctr, kMaxBands));
+  CK(cudaMemsetAsync(r->rb.ctr, 0, sizeof(DevCounters) * kMaxBands, r->st));
+  r->rb.lctr = r->rb.ctr;
+  r->rb.base = 0;
+  r->rb.count = (uint32_t)np;
   CK(cudaMemsetAsync(r->rb.cache[0], 0, (size_t)cacheCap * 96, r->st));
   CK(cudaMemsetAsync(r->rb.cache[1], 0, (size_t)cacheCap * 96, r->st));
   r->rb.cap = (uint32_t)cap;
@@ -704,30 +753,56 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
       } else
         CK(launch_adapt_budget(a, r->rb, r->ab, r->result, r->sampleN, r->p.desired_n, st));
       mark(r, kPhAdapt, tm);
-    } else {
-      CK(launch_camera(a, r->rb, st));
-      mark(r, kPhOther, tm);
     }
     // bounce d < K: walk (extension rays of d + shadow rays of d-1), then shade
     // d, one launch each; bounces >= K: one persistent kernel per frame carries
     // every remaining path to its end (few paths are left by then, and per-bounce
     // launches would each wait for their slowest ray)
-    int in = 0;
     const uint32_t D = a.eyeDepth;
     const uint32_t K = std::min(tail_from(D, S.traversal == 1 && S.wide, r->p.tail_from), D);
-    for (uint32_t d = 0; d < K; d++) {
-      CK(launch_walk(S, a, r->rb, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), d == 1, st));
-      mark(r, kPhTrace, tm);
-      CK(launch_shade(S, a, r->rb, in, d, K < D && d + 1 == K, st));
-      mark(r, kPhShade, tm);
-      in ^= 1;
-    }
-    if (K < D) {
-      CK(launch_tail(S, a, r->rb, in, K > 0 ? (int)((K - 1) & 1u) : -1, K, st));
+    auto bounces = [&](const RenderBuffers& rbx, cudaStream_t sx, bool mk) -> gbpt_status {
+      int in = 0;
+      for (uint32_t d = 0; d < K; d++) {
+        CK(launch_walk(S, a, rbx, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), d == 1, sx));
+        if (mk) mark(r, kPhTrace, tm);
+        CK(launch_shade(S, a, rbx, in, d, K < D && d + 1 == K, sx));
+        if (mk) mark(r, kPhShade, tm);
+        in ^= 1;
+      }
+      if (K < D) {
+        CK(launch_tail(S, a, rbx, in, K > 0 ? (int)((K - 1) & 1u) : -1, K, sx));
+      } else {
+        // shadow rays of the last bounce (none in practice: paths at the depth cap
+        // terminate without connecting; kept so the sequence needs no special case)
+        CK(launch_walk(S, a, rbx, -1, (int)((D - 1) & 1u), (int)(D & 1u), D == 1, sx));
+      }
+      return GBPT_OK;
+    };
+    const size_t np = (size_t)r->W * r->H;
+    const uint32_t nb = adaptive ? 1u : bands_for(r->p.bands, np);
+    r->lastBands = nb;
+    if (budgeted || nb == 1) {
+      if (!budgeted) {
+        CK(launch_camera(a, r->rb, st));
+        mark(r, kPhOther, tm);
+      }
+      gbpt_status be = bounces(r->rb, st, true);
+      if (be != GBPT_OK) return be;
     } else {
-      // shadow rays of the last bounce (none in practice: paths at the depth cap
-      // terminate without connecting; kept so the sequence needs no special case)
-      CK(launch_walk(S, a, r->rb, -1, (int)((D - 1) & 1u), (int)(D & 1u), D == 1, st));
+      // one wavefront per band: camera rays and every bounce of the band on its
+      // own stream; the apply below waits for all of them.  Results do not
+      // depend on the split: every path's random numbers follow from its pixel.
+      CK(cudaEventRecord(r->evFork, st));
+      for (uint32_t b = 0; b < nb; b++) {
+        cudaStream_t sb = r->stBand[b];
+        CK(cudaStreamWaitEvent(sb, r->evFork, 0));
+        const RenderBuffers rbb = band_buffers(r->rb, b, nb, np);
+        CK(launch_camera(a, rbb, sb));
+        gbpt_status be = bounces(rbb, sb, false);
+        if (be != GBPT_OK) return be;
+        CK(cudaEventRecord(r->evJoin[b], sb));
+      }
+      for (uint32_t b = 0; b < nb; b++) CK(cudaStreamWaitEvent(st, r->evJoin[b], 0));
     }
     mark(r, kPhTrace, tm);
     if (budgeted) {
@@ -810,9 +885,23 @@ struct CtrSnap {
   unsigned long long rays, nodes, tris;
 };
 
+// The renderer's counters with the bands' work counters, paths and error
+// words added into the first band's.
 gbpt_status read_ctr(gbpt_renderer* r, DevCounters* out) {
-  CK(cudaMemcpyAsync(out, r->rb.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, r->st));
+  DevCounters c[kMaxBands];
+  CK(cudaMemcpyAsync(c, r->rb.ctr, sizeof(c), cudaMemcpyDeviceToHost, r->st));
   CK(cudaStreamSynchronize(r->st));
+  *out = c[0];
+  for (uint32_t b = 1; b < kMaxBands; b++) {
+    out->rays += c[b].rays;
+    out->nodes += c[b].nodes;
+    out->tris += c[b].tris;
+    out->shadowRays += c[b].shadowRays;
+    out->nodesS += c[b].nodesS;
+    out->trisS += c[b].trisS;
+    out->errFlags |= c[b].errFlags;
+    if (b < r->lastBands) out->paths += c[b].paths;
+  }
   return GBPT_OK;
 }
 
@@ -852,12 +941,14 @@ gbpt_status render_impl(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam,
                              r->st));
   CK(cudaStreamSynchronize(r->st));
   CK(cudaGetLastError());
-  {  // device-side error words (bounded waits, bounds checks): report once, then clear
+  {  // device-side error words (bounded waits, bounds checks) of every band: report once, then clear
     uint32_t flags = 0;
-    CK(cudaMemcpyAsync(&flags, &r->rb.ctr->errFlags, 4, cudaMemcpyDeviceToHost, r->st));
-    CK(cudaStreamSynchronize(r->st));
+    DevCounters c{};
+    stt = read_ctr(r, &c);
+    if (stt != GBPT_OK) return stt;
+    flags = c.errFlags;
     if (flags) {
-      CK(cudaMemsetAsync(&r->rb.ctr->errFlags, 0, 4, r->st));
+      for (uint32_t b = 0; b < kMaxBands; b++) CK(cudaMemsetAsync(&r->rb.ctr[b].errFlags, 0, 4, r->st));
       CK(cudaStreamSynchronize(r->st));
       if (flags & 4u) return fail(GBPT_ERR_TIMEOUT, "grid barrier of the binary allocator timed out");
       if (flags & kErrMlpTimeout) return fail(GBPT_ERR_TIMEOUT, "learned allocator: tensor-core wait timed out");
@@ -1015,6 +1106,7 @@ gbpt_status gbpt_params_default(gbpt_params* p) {
   p->pt_depth_max = 10;
   p->walk_refill = 0;
   p->tail_from = -1;
+  p->bands = 0;
   return GBPT_OK;
 }
 
@@ -1214,6 +1306,15 @@ gbpt_status gbpt_renderer_create(uint32_t width, uint32_t height, int32_t mode, 
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->evMain, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->evLight[0], cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->evLight[1], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->evFork, cudaEventDisableTiming);
+  // band b's stream has the b-th highest priority: the first band takes the
+  // SMs whenever it has work and the others fill what its walks leave idle,
+  // so the bands run out of phase
+  for (uint32_t b = 0; b < kMaxBands && e == cudaSuccess; b++) {
+    e = cudaEventCreateWithFlags(&r->evJoin[b], cudaEventDisableTiming);
+    const int pr = std::min(prHigh + (int)b, prLow);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&r->stBand[b], cudaStreamNonBlocking, pr);
+  }
   if (e != cudaSuccess) {
     delete r;
     return fail(GBPT_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));

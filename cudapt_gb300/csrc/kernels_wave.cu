@@ -334,17 +334,19 @@ __global__ void __launch_bounds__(1024) k_light(DevScene S, FrameArgs a, float4*
 }
 
 // ---------------------------------------------------------------------------
-// Camera rays, one per pixel (pt_genPathQueue_kernel, :619-640).
+// Camera rays, one per pixel (pt_genPathQueue_kernel, :619-640), for the
+// band's pixels b.base .. b.base + b.count - 1; a ray's wave index is its
+// index inside the band.
 __global__ void k_camera(FrameArgs a, RenderBuffers b) {
   using namespace gb;
-  const uint32_t np = a.width * a.height;
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p == 0) {
-    b.ctr->wave[0] = np;
-    b.ctr->paths = np;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    b.ctr->wave[0] = b.count;
+    b.ctr->paths = b.count;
     b.ctr->fetchT = 0;
   }
-  if (p >= np) return;
+  if (i >= b.count) return;
+  const uint32_t p = b.base + i;
   const uint32_t x = p % a.width, y = p / a.width;
   float u[4];
   draw4(a.key0, a.key1, p, a.frame, kCamera, 0, 0, 0, u);
@@ -358,10 +360,10 @@ __global__ void k_camera(FrameArgs a, RenderBuffers b) {
   f3 D = mk(a.camDir[0], a.camDir[1], a.camDir[2]);
   f3 dir = normalize((R * au + U * av) + D);
   Wave w = b.wave[0];
-  w.o[p] = make_float4(a.camPos[0], a.camPos[1], a.camPos[2], __uint_as_float(p));
-  w.d[p] = st4u(dir, p);
-  w.thr[p] = make_float4(1.f, 1.f, 1.f, 1.f);  // .w: path potential (filter-only mode)
-  w.smp[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+  w.o[i] = make_float4(a.camPos[0], a.camPos[1], a.camPos[2], __uint_as_float(p));
+  w.d[i] = st4u(dir, p);
+  w.thr[i] = make_float4(1.f, 1.f, 1.f, 1.f);  // .w: path potential (filter-only mode)
+  w.smp[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   b.res[p] = make_float4(0.f, 0.f, 0.f, __uint_as_float(0u));
   b.slotPix[p] = p;
   b.slotSmp[p] = 0;
@@ -615,7 +617,7 @@ __device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a
 __global__ void __launch_bounds__(kBlock, 3) k_shade(DevScene S, FrameArgs a, RenderBuffers b, int in, uint32_t depth,
                                                      uint32_t attach) {
   const uint32_t n = b.ctr->wave[in];
-  const uint32_t cacheSize = b.ctr->cacheSize[a.cacheSel];
+  const uint32_t cacheSize = b.lctr->cacheSize[a.cacheSel];
   const float4* __restrict__ cache = b.cache[a.cacheSel];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     atomicAdd(&b.ctr->rays, (unsigned long long)n);
@@ -695,7 +697,7 @@ template <bool kCount, bool kWide>
 __global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, RenderBuffers b, int in, int shIn,
                                                    uint32_t depth0, uint32_t kRefill) {
   const uint32_t n = b.ctr->wave[in];
-  const uint32_t cacheSize = b.ctr->cacheSize[a.cacheSel];
+  const uint32_t cacheSize = b.lctr->cacheSize[a.cacheSel];
   const float4* __restrict__ cache = b.cache[a.cacheSel];
   const float4* __restrict__ sh = b.sh[shIn >= 0 ? shIn : 0];
   const Wave wv = b.wave[in];
@@ -984,8 +986,7 @@ cudaError_t launch_light_pass(const DevScene& S, const FrameArgs& a, const Rende
 }
 
 cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream_t st) {
-  const uint32_t np = a.width * a.height;
-  k_camera<<<(np + kBlock - 1) / kBlock, kBlock, 0, st>>>(a, b);
+  k_camera<<<(b.count + kBlock - 1) / kBlock, kBlock, 0, st>>>(a, b);
   note_launches(1);
   return cudaGetLastError();
 }

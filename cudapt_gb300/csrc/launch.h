@@ -100,10 +100,18 @@ struct RenderBuffers {
   uint32_t* slotSmp;    // per slot sample id
   float4* cache[2];     // two light-vertex caches (6 float4 per vertex): one is read by the
                         // current frames while the next light pass fills the other
-  DevCounters* ctr;
+  DevCounters* ctr;     // this band's queue counters (the renderer's first counters without bands)
+  DevCounters* lctr;    // the counters the light pass writes the cache sizes to (the renderer's first)
   uint32_t cap;         // slots
   uint32_t cacheCap;    // light vertices
+  // Band of camera paths this wavefront carries: pixels base .. base+count-1.
+  // A frame split into bands runs one wavefront per band on its own stream;
+  // wave, hit and connection-queue pointers then point at the band's part of
+  // the renderer's buffers, and per-slot arrays stay indexed by pixel.
+  uint32_t base;
+  uint32_t count;
 };
+constexpr uint32_t kMaxBands = 8;
 
 // wavefront kernels (kernels_wave.cu)
 cudaError_t launch_light_pass(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, cudaStream_t st);

@@ -67,6 +67,7 @@ PARAMS = np.dtype(
         ("pt_depth_max", "<u4"),
         ("walk_refill", "<u4"),
         ("tail_from", "<i4"),
+        ("bands", "<u4"),
     ]
 )
 
@@ -118,6 +119,7 @@ def default_params(**over):
     p["pt_depth_max"] = 10
     p["walk_refill"] = 0
     p["tail_from"] = -1
+    p["bands"] = 0
     for k, v in over.items():
         p[k] = v
     return p

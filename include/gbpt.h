@@ -105,6 +105,8 @@ typedef struct gbpt_params {
                                (1..32; 0: 8 in the reference order, 20 in the wide order) */
   int32_t tail_from;        /* first bounce the per-path tail kernel carries (>= the depth cap: none;
                                -1: depth / 2 - 1 (wide order: depth / 2) when the cap exceeds 6, else none) */
+  uint32_t bands;           /* wavefronts a frame's camera paths are split into, each on its own stream
+                               (1..8; 0: 2 from 512K paths, else 1); the adaptive modes use 1 */
 } gbpt_params;
 
 /* Renderer modes: the BDPT entries of the X-macro registry

@@ -349,3 +349,37 @@ def test_graph_frames_equal_direct_launches(gbdev, mode, depth):
         r.close()
     for f, (a, b) in enumerate(zip(*runs)):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), f
+
+
+@pytest.mark.parametrize("mode", [0, 3, 4])
+def test_bands_change_no_pixel(gbdev, orc, mode):
+    """A frame split into bands (one wavefront per band, each on its own
+    stream) gives the image of a single wavefront, with and without CUDA
+    graphs; the stats count every band's paths and rays."""
+    (v, t, m), cam = scene_arrays("interior")
+    s = gbdev.RTScene(v, t, m).build_bvh()
+    W, H = 97, 61  # bands of unequal size
+    imgs, stats = {}, {}
+    for bands in (1, 2, 3, 8):
+        for graphs in (False, True):
+            p = gbdev.default_params(eye_depth_max=10, light_depth_max=10, pt_depth_max=8, bands=bands,
+                                     render_iterations=3)
+            r = gbdev.RTRenderer(W, H, mode, p)
+            r.set_graphs(graphs)
+            for _ in range(4):
+                img = r.render(s, cam).copy()
+            imgs[bands, graphs] = (r.read_buffer(0), r.read_buffer(6))
+            stats[bands, graphs] = r.last_stats
+            r.close()
+    base = imgs[1, False]
+    for key, (res, sn) in imgs.items():
+        assert_bits_equal(res, base[0], f"image, bands/graphs {key}")
+        assert_bits_equal(sn, base[1], f"sampleN, bands/graphs {key}")
+    for key, st in stats.items():
+        if mode != 3:  # the filter-only mode's fourth frame only filters
+            assert st["paths"] == W * H, (key, st["paths"])
+            assert st["rays"] == stats[1, False]["rays"], key
+    ref = orc.Renderer(W, H, mode, gbdev.default_params(eye_depth_max=10, light_depth_max=10, pt_depth_max=8,
+                                                         render_iterations=3))
+    ref.render(orc.Scene(v, t, m), cam, 4)
+    assert_bits_equal(base[0], ref.get(0), "image against the oracle")

@@ -470,7 +470,10 @@ def serving_run(gb, n=64, rate=200.0, seed=0, workers=4):
     low_rate = round(0.6 * cap, 2)
     low, _ = serving.run_poisson(gb, serving.poisson_workload(n, low_rate, seed), objs, cams, workers=workers)
     low["rate_per_s"] = low_rate
+    # the saturated run again with one worker: the gain of running requests side by side
+    one, _ = serving.run_poisson(gb, wl, objs, cams, workers=1)
     out = {"saturated": summary, "below_saturation": low,
+           "saturated_one_worker": {k: one[k] for k in ("mpaths_per_s", "wall_s", "p50_ms", "p99_ms")},
            "capacity_requests_per_s": round(cap, 2),
            "config": (f"{n} requests, Poisson {rate:g}/s and 0.6x measured capacity (seed {seed}), scenes "
                       "cornell/interior/hall, resolution in {128^2, 256^2, 512^2, 1024x768}, spp in {4, 16, 64}, "

@@ -211,6 +211,12 @@ class RTRenderer:
         self._mode = int(np.frombuffer(data[20:24], np.int32)[0])  # the header's mode word
         return self
 
+    def set_window(self, x0, y0, full_w, full_h):
+        """Render the window at (x0, y0) of a full_w x full_h image (rays and random
+        numbers of the full image's pixels); (0, 0, width, height) is the whole image."""
+        check(load().gbpt_renderer_set_window(self._h, int(x0), int(y0), int(full_w), int(full_h)))
+        return self
+
     def set_graphs(self, on=True):
         """Issue each frame of the plain and PTSC modes as one CUDA graph (same image)."""
         check(load().gbpt_renderer_set_graphs(self._h, 1 if on else 0))

@@ -115,6 +115,7 @@ SIGNATURES = {
     "gbpt_renderer_create": (i32, [u32, u32, i32, vp, vp]),
     "gbpt_renderer_destroy": (i32, [vp]),
     "gbpt_set_mode": (i32, [vp, i32]),
+    "gbpt_renderer_set_window": (i32, [vp, u32, u32, u32, u32]),
     "gbpt_set_params": (i32, [vp, vp]),
     "gbpt_get_params": (i32, [vp, vp]),
     "gbpt_render": (i32, [vp, vp, vp, vp, i32, vp]),
@@ -137,6 +138,7 @@ SIGNATURES = {
     "gbpt_server_submit": (i32, [vp, vp, vp]),
     "gbpt_server_wait": (i32, [vp, ctypes.c_uint64, u32, vp]),
     "gbpt_server_tuned": (i32, [vp, i32, u32, u32, u32, vp, vp, vp]),
+    "gbpt_server_tuned_params": (i32, [vp, i32, u32, u32, u32, vp, vp]),
     "gbpt_reset": (i32, [vp]),
     "gbpt_clean": (i32, [vp]),
     "gbpt_set_counting": (i32, [vp, i32]),

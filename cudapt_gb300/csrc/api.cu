@@ -316,6 +316,8 @@ struct gbpt_renderer {
   cudaStream_t stBand[kMaxBands] = {};
   cudaEvent_t evFork = nullptr, evJoin[kMaxBands] = {};
   uint32_t lastBands = 1;
+  // window of a larger image (gbpt_renderer_set_window); the whole image by default
+  uint32_t winX0 = 0, winY0 = 0, fullW = 0, fullH = 0;
   // frames issued as CUDA graphs (plain and PTSC modes): executable graphs
   // without / with an inline light pass
   bool graphs = false, graphWarm = false;
@@ -416,6 +418,7 @@ gbpt_status check_params(const gbpt_params* p) {
   if (p->walk_refill > 32) return fail(GBPT_ERR_INVALID_ARG, "walk_refill must be 0..32");
   if (p->tail_from < -1) return fail(GBPT_ERR_INVALID_ARG, "tail_from must be >= -1");
   if (p->bands > kMaxBands) return fail(GBPT_ERR_INVALID_ARG, "bands must be 0..8");
+  if (p->walk_ctas > 32) return fail(GBPT_ERR_INVALID_ARG, "walk_ctas must be 0..32");
   return GBPT_OK;
 }
 
@@ -645,10 +648,14 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
     a.camRight[k] = right[k];
   }
   a.tanHalf = (float)std::tan((double)(cam->fov * 0.5f));
-  a.W = (float)r->W;
-  a.H = (float)r->H;
+  const uint32_t fullW = r->fullW ? r->fullW : r->W, fullH = r->fullH ? r->fullH : r->H;
+  a.W = (float)fullW;
+  a.H = (float)fullH;
   a.width = r->W;
   a.height = r->H;
+  a.winX0 = r->winX0;
+  a.winY0 = r->winY0;
+  a.fullW = fullW;
   a.frame = r->frame;
   a.key0 = r->p.seed;
   a.key1 = r->p.request_id;
@@ -661,6 +668,9 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   a.useEnv = (r->p.env[0] != 0.f || r->p.env[1] != 0.f || r->p.env[2] != 0.f) ? 1u : 0u;
   const bool adaptive = r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT || r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY;
   const bool binary = r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT_BINARY;
+  if (adaptive && (fullW != r->W || fullH != r->H))
+    return fail(GBPT_ERR_STATE, "the adaptive modes render whole images only: their sample budget and filter "
+                                "couple every pixel of the image");
   // the PLL variant pushes the specular origin along reflDir (AdapBilatAtomic.cu:583); the others do not
   a.specPush = r->mode == GBPT_MODE_BDPT_SC_ADAP_BILAT ? 1u : 0u;
   const bool bilat = r->mode == GBPT_MODE_BDPT_SC_BILAT;
@@ -671,6 +681,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   a.moments = (learned || (r->collect && adaptive)) ? 1u : 0u;
   a.tilesX = (r->W + 7) / 8;
   a.refill = r->p.walk_refill;
+  a.walkCtas = r->p.walk_ctas;
   if (a.moments && r->frame == 0)
     CK(cudaMemsetAsync(r->rb.hist, 0, (size_t)a.tilesX * ((r->H + 7) / 8) * 32, r->st));
   a.counting = r->counting ? 1u : 0u;
@@ -1107,6 +1118,7 @@ gbpt_status gbpt_params_default(gbpt_params* p) {
   p->walk_refill = 0;
   p->tail_from = -1;
   p->bands = 0;
+  p->walk_ctas = 0;
   return GBPT_OK;
 }
 
@@ -1463,6 +1475,22 @@ gbpt_status gbpt_renderer_set_stream(gbpt_renderer* r, void* stream) {
   if (!r->ownSt) r->ownSt = r->st;
   r->st = stream ? (cudaStream_t)stream : r->ownSt;
   r->userStream = stream != nullptr;
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_renderer_set_window(gbpt_renderer* r, uint32_t x0, uint32_t y0, uint32_t full_w, uint32_t full_h) {
+  if (!r) return fail(GBPT_ERR_INVALID_ARG, "renderer is NULL");
+  if (full_w == 0 || full_h == 0 || (uint64_t)full_w * full_h > (1ull << 32) - 1 || x0 > full_w ||
+      y0 > full_h || r->W > full_w - x0 || r->H > full_h - y0)
+    return fail(GBPT_ERR_INVALID_ARG, "the renderer's " + std::to_string(r->W) + "x" + std::to_string(r->H) +
+                                          " window at (" + std::to_string(x0) + ", " + std::to_string(y0) +
+                                          ") does not fit a " + std::to_string(full_w) + "x" +
+                                          std::to_string(full_h) + " image");
+  r->winX0 = x0;
+  r->winY0 = y0;
+  r->fullW = full_w;
+  r->fullH = full_h;
+  r->started = false;  // progressive accumulation restarts
   return GBPT_OK;
 }
 

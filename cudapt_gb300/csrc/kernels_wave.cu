@@ -20,6 +20,7 @@
 //
 // Queue lengths live in device memory (DevCounters) and every kernel runs a
 // grid-stride loop over them, so the host never waits on a count.
+#include <algorithm>
 #include <atomic>
 #include <cuda_runtime.h>
 
@@ -347,9 +348,12 @@ __global__ void k_camera(FrameArgs a, RenderBuffers b) {
   }
   if (i >= b.count) return;
   const uint32_t p = b.base + i;
-  const uint32_t x = p % a.width, y = p / a.width;
+  // pixel of the full image: its coordinates place the ray and its id keys
+  // every random number of the path, so a window renders as in the full image
+  const uint32_t x = a.winX0 + p % a.width, y = a.winY0 + p / a.width;
+  const uint32_t gp = y * a.fullW + x;
   float u[4];
-  draw4(a.key0, a.key1, p, a.frame, kCamera, 0, 0, 0, u);
+  draw4(a.key0, a.key1, gp, a.frame, kCamera, 0, 0, 0, u);
   const float W = a.W, H = a.H, th = a.tanHalf;
   float cu = ((((2.f * ((float)x + 0.5f)) / W) - 1.f) * th * W) / H;
   float cv = (((2.f * ((float)y + 0.5f)) / H) - 1.f) * th;
@@ -361,7 +365,7 @@ __global__ void k_camera(FrameArgs a, RenderBuffers b) {
   f3 dir = normalize((R * au + U * av) + D);
   Wave w = b.wave[0];
   w.o[i] = make_float4(a.camPos[0], a.camPos[1], a.camPos[2], __uint_as_float(p));
-  w.d[i] = st4u(dir, p);
+  w.d[i] = st4u(dir, gp);
   w.thr[i] = make_float4(1.f, 1.f, 1.f, 1.f);  // .w: path potential (filter-only mode)
   w.smp[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   b.res[p] = make_float4(0.f, 0.f, 0.f, __uint_as_float(0u));
@@ -1009,17 +1013,24 @@ uint32_t shade_grid() {
   return g;
 }
 
+// persistent grid: every CTA that fits, or `ctasPerSm` per SM when that is
+// fewer (requests that share the GPU leave SMs to each other)
+uint32_t persistent_grid(uint32_t full, uint32_t ctasPerSm) {
+  if (ctasPerSm == 0) return full;
+  return std::min(full, (uint32_t)sm_count() * ctasPerSm);
+}
+
 template <bool kCount, bool kWide>
 void walk_variant(const DevScene& S, const RenderBuffers& b, int in, int shIn, int shReset, uint32_t sd,
-                  uint32_t refill, cudaStream_t st) {
-  const uint32_t g = walk_grid<kCount, kWide>();
+                  uint32_t refill, uint32_t ctas, cudaStream_t st) {
+  const uint32_t g = persistent_grid(walk_grid<kCount, kWide>(), ctas);
   k_walk<kCount, kWide><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, sd, refill);
 }
 
 template <bool kCount, bool kWide>
 void tail_variant(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn, uint32_t depth0,
                   cudaStream_t st) {
-  const uint32_t g = tail_grid<kCount, kWide>();
+  const uint32_t g = persistent_grid(tail_grid<kCount, kWide>(), a.walkCtas);
   k_tail<kCount, kWide><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill_for(a.refill, kWide));
 }
 
@@ -1029,11 +1040,11 @@ cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffe
   const bool wide = S.traversal == 1 && S.wide;
   const uint32_t rf = walk_refill_for(a.refill, wide);
   if (a.counting) {
-    if (wide) walk_variant<true, true>(S, b, in, shIn, shReset, sd, rf, st);
-    else walk_variant<true, false>(S, b, in, shIn, shReset, sd, rf, st);
+    if (wide) walk_variant<true, true>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, st);
+    else walk_variant<true, false>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, st);
   } else {
-    if (wide) walk_variant<false, true>(S, b, in, shIn, shReset, sd, rf, st);
-    else walk_variant<false, false>(S, b, in, shIn, shReset, sd, rf, st);
+    if (wide) walk_variant<false, true>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, st);
+    else walk_variant<false, false>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, st);
   }
   note_launches(1);
   return cudaGetLastError();

@@ -83,6 +83,12 @@ struct FrameArgs {
   uint32_t moments;     // learned allocator: per-pixel second moments and per-tile path-length counts
   uint32_t tilesX;      // 8x8 tiles per image row
   uint32_t refill;      // idle lanes of a warp that trigger a refill in the persistent walks
+  uint32_t walkCtas;    // CTAs per SM of the persistent walk and tail grids (0: as many as fit)
+  // window of a larger image this renderer covers (gbpt_renderer_set_window):
+  // local pixel (x, y) is pixel (winX0 + x, winY0 + y) of a fullW-wide image;
+  // W and H above are the full image's for the camera projection, width and
+  // height the window's
+  uint32_t winX0, winY0, fullW;
 };
 
 struct RenderBuffers {

@@ -19,11 +19,13 @@
 // renderers, then waits for running requests to finish, and fails the request
 // with GBPT_ERR_OOM only when no other request is running.
 //
-// Autotuning: the walks' refill threshold and the bounce from which the tail
-// kernel carries the remaining paths change scheduling only -- every path
-// executes the same operations in the same order -- so images are identical
-// whichever values run.  Requests that leave them at their defaults
-// (walk_refill 0, tail_from -1) are assigned a candidate per class (mode,
+// Autotuning: the walks' refill threshold, the bounce from which the tail
+// kernel carries the remaining paths, the bands a frame is split into and the
+// persistent grids' CTAs per SM change scheduling and launch shape only --
+// every path executes the same operations in the same order -- so images are
+// identical whichever values run.  Requests that leave them at their defaults
+// (walk_refill 0, tail_from -1, bands 0, walk_ctas 0) are assigned a candidate
+// per class (mode,
 // depth cap, image size rounded to a power of two); each candidate is timed
 // on whole requests (device time per camera path) until it has kTrials
 // samples, after which the class uses the fastest.
@@ -63,18 +65,29 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
 
 struct Knobs {
   uint32_t refill;
-  int32_t tail;  // -1: the library's rule
+  int32_t tail;    // -1: the library's rule
+  uint32_t bands;  // wavefronts per frame
+  uint32_t ctas;   // CTAs per SM of the persistent walk and tail grids (0: as many as fit)
+  bool operator==(const Knobs& o) const {
+    return refill == o.refill && tail == o.tail && bands == o.bands && ctas == o.ctas;
+  }
 };
 
-// Candidates per class: the library default first, then the refill
-// thresholds and wavefront depths around it that measured within a few
-// percent on the large workloads (small images favour earlier refills and
-// earlier tails, whose per-bounce launches wait on their slowest ray).
-std::vector<Knobs> candidates(uint32_t depth) {
-  std::vector<Knobs> c = {{8, -1}, {4, -1}, {16, -1}};
-  if (depth > 3) c.push_back({8, (int32_t)depth - 3});
-  if (depth > 5) c.push_back({8, (int32_t)depth - 5});
-  c.push_back({8, (int32_t)depth});  // no tail kernel
+// Candidates per class: the library default first (one band: concurrent
+// requests already overlap each other's walks), then the refill thresholds
+// and wavefront depths around it that measured within a few percent on the
+// large workloads (small images favour earlier refills and earlier tails,
+// whose per-bounce launches wait on their slowest ray), then launch shapes:
+// persistent grids of 2 or 3 CTAs per SM, which leave SMs to the requests
+// running beside, and two bands for images of 512K pixels and more.
+std::vector<Knobs> candidates(uint32_t depth, uint32_t sizeLog2) {
+  std::vector<Knobs> c = {{8, -1, 1, 0}, {4, -1, 1, 0}, {16, -1, 1, 0}};
+  if (depth > 3) c.push_back({8, (int32_t)depth - 3, 1, 0});
+  if (depth > 5) c.push_back({8, (int32_t)depth - 5, 1, 0});
+  c.push_back({8, (int32_t)depth, 1, 0});  // no tail kernel
+  c.push_back({8, -1, 1, 2});
+  c.push_back({8, -1, 1, 3});
+  if (sizeLog2 >= 19) c.push_back({8, -1, 2, 0});
   return c;
 }
 
@@ -104,7 +117,7 @@ struct Request {
   gbpt_request q{};
   gbpt_params p{};
   bool tuned = false;  // knobs come from the autotuner
-  Knobs knobs{0, -1};
+  Knobs knobs{0, -1, 0, 0};
   Clock::time_point tSubmit, tStart, tEnd;
   gbpt_status status = GBPT_OK;
   std::string err;
@@ -156,7 +169,7 @@ struct gbpt_server {
   Knobs assign(const ClassKey& k) {
     Tuning& t = tuning[k];
     if (t.cand.empty()) {
-      t.cand = candidates(k.depth);
+      t.cand = candidates(k.depth, k.size);
       t.msPerPath.assign(t.cand.size(), 0.0);
       t.trials.assign(t.cand.size(), 0);
     }
@@ -187,7 +200,7 @@ struct gbpt_server {
   void record(const ClassKey& k, const Knobs& kn, double msPerPath) {
     Tuning& t = tuning[k];
     for (size_t i = 0; i < t.cand.size(); i++)
-      if (t.cand[i].refill == kn.refill && t.cand[i].tail == kn.tail) {
+      if (t.cand[i] == kn) {
         t.msPerPath[i] += msPerPath;
         t.trials[i]++;
       }
@@ -239,6 +252,8 @@ static gbpt_status run_request(gbpt_server* srv, Pool& pool, Request& q, std::st
   if (q.tuned) {
     p.walk_refill = q.knobs.refill;
     p.tail_from = q.knobs.tail;
+    p.bands = q.knobs.bands;
+    p.walk_ctas = q.knobs.ctas;
   }
   gbpt_renderer* r = nullptr;
   {
@@ -387,8 +402,8 @@ gbpt_status gbpt_server_submit(gbpt_server* s, const gbpt_request* req, uint64_t
   } else {
     gbpt_params_default(&q->p);
   }
-  q->tuned = q->p.walk_refill == 0 && q->p.tail_from == -1;
-  q->knobs = Knobs{q->p.walk_refill, q->p.tail_from};
+  q->tuned = q->p.walk_refill == 0 && q->p.tail_from == -1 && q->p.bands == 0 && q->p.walk_ctas == 0;
+  q->knobs = Knobs{q->p.walk_refill, q->p.tail_from, q->p.bands, q->p.walk_ctas};
   q->tSubmit = Clock::now();
   {
     std::lock_guard<std::mutex> lock(s->mu);
@@ -431,6 +446,34 @@ gbpt_status gbpt_server_release(gbpt_server* s, uint64_t id) {
   if (it == s->reqs.end()) return fail(GBPT_ERR_INVALID_ARG, "unknown request id");
   if (!it->second->done) return fail(GBPT_ERR_STATE, "request still queued or running");
   s->reqs.erase(it);
+  return GBPT_OK;
+}
+
+gbpt_status gbpt_server_tuned_params(gbpt_server* s, int32_t mode, uint32_t depth, uint32_t width, uint32_t height,
+                                     gbpt_params* knobs, uint32_t* samples) {
+  if (!s || !knobs || !samples) return fail(GBPT_ERR_INVALID_ARG, "NULL argument");
+  gbpt_params_default(knobs);
+  Request probe;
+  probe.q.width = width;
+  probe.q.height = height;
+  std::lock_guard<std::mutex> lock(s->mu);
+  auto it = s->tuning.find(ClassKey{mode, depth, probe.size()});
+  *samples = 0;
+  if (it == s->tuning.end()) {
+    const Knobs k = candidates(depth, probe.size())[0];
+    knobs->walk_refill = k.refill;
+    knobs->tail_from = k.tail;
+    knobs->bands = k.bands;
+    knobs->walk_ctas = k.ctas;
+    return GBPT_OK;
+  }
+  const Tuning& t = it->second;
+  const Knobs& k = t.cand[gbpt_server::best(t)];
+  knobs->walk_refill = k.refill;
+  knobs->tail_from = k.tail;
+  knobs->bands = k.bands;
+  knobs->walk_ctas = k.ctas;
+  for (uint32_t n : t.trials) *samples += n;
   return GBPT_OK;
 }
 

@@ -68,6 +68,7 @@ PARAMS = np.dtype(
         ("walk_refill", "<u4"),
         ("tail_from", "<i4"),
         ("bands", "<u4"),
+        ("walk_ctas", "<u4"),
     ]
 )
 
@@ -120,6 +121,7 @@ def default_params(**over):
     p["walk_refill"] = 0
     p["tail_from"] = -1
     p["bands"] = 0
+    p["walk_ctas"] = 0
     for k, v in over.items():
         p[k] = v
     return p

@@ -77,6 +77,16 @@ class Server:
                                        ctypes.addressof(r), ctypes.addressof(t), ctypes.addressof(n)))
         return r.value, t.value, n.value
 
+    def tuned_knobs(self, mode, depth, width, height):
+        """Every knob the autotuner holds for a request class: dict(walk_refill,
+        tail_from, bands, walk_ctas, samples)."""
+        p = layouts.default_params()
+        n = ctypes.c_uint32()
+        check(load().gbpt_server_tuned_params(self._h, int(mode), int(depth), int(width), int(height),
+                                              p.ctypes.data, ctypes.addressof(n)))
+        return dict(walk_refill=int(p["walk_refill"]), tail_from=int(p["tail_from"]), bands=int(p["bands"]),
+                    walk_ctas=int(p["walk_ctas"]), samples=n.value)
+
     def close(self):
         """Finishes queued and running requests, then frees the renderers."""
         if getattr(self, "_h", None) and self._h.value:
@@ -126,12 +136,13 @@ def run_poisson(gb, workload, scene_objs, cameras, workers=4, hbm_reserve=1 << 3
             for i in ids:
                 srv.wait(i)
         t0 = time.perf_counter()
-        ids = []
+        ids, submitted = [], []
         for (at, name, w, h, spp, depth), (arr, _) in zip(workload, bufs):
             now = time.perf_counter() - t0
             if at > now:
                 time.sleep(at - now)
             p = gb.default_params(eye_depth_max=depth, light_depth_max=depth)
+            submitted.append(time.perf_counter() - t0)
             ids.append(srv.submit(scene_objs[name], cameras[name], w, h, spp, params=p, out=arr))
         st = [srv.wait(i) for i in ids]
         wall = time.perf_counter() - t0
@@ -154,5 +165,32 @@ def run_poisson(gb, workload, scene_objs, cameras, workers=4, hbm_reserve=1 << 3
         "workers": workers,
         "policy": "shortest first (aging)" if policy == Server.SHORTEST_FIRST else "fifo",
         "graphs": bool(graphs),
+        "overlap": overlap(submitted, st, wall),
     }
     return summary, st
+
+
+def overlap(submitted, statuses, wall):
+    """How far requests ran side by side: each request runs from submit +
+    queued_ms to submit + latency_ms; the share of the wall time with 0, 1, 2,
+    ... requests running, the mean number running while any runs, and the
+    summed run time over the wall time."""
+    ev = []
+    for t, s in zip(submitted, statuses):
+        ev.append((t + s["queued_ms"] / 1e3, 1))
+        ev.append((t + s["latency_ms"] / 1e3, -1))
+    ev.sort()
+    share, busy, run_sum = {}, 0.0, 0.0
+    k, last = 0, 0.0
+    for t, d in ev:
+        span = max(t - last, 0.0)
+        share[k] = share.get(k, 0.0) + span
+        if k:
+            busy += span
+            run_sum += span * k
+        k += d
+        last = t
+    share[0] = share.get(0, 0.0) + max(wall - last, 0.0)
+    return {"share_of_wall_running": {str(n): round(v / wall, 3) for n, v in sorted(share.items())},
+            "mean_running_while_busy": round(run_sum / busy, 2) if busy else 0.0,
+            "run_time_over_wall": round(sum(s["run_ms"] for s in statuses) / 1e3 / wall, 2)}

@@ -107,6 +107,8 @@ typedef struct gbpt_params {
                                -1: depth / 2 - 1 (wide order: depth / 2) when the cap exceeds 6, else none) */
   uint32_t bands;           /* wavefronts a frame's camera paths are split into, each on its own stream
                                (1..8; 0: 2 from 512K paths, else 1); the adaptive modes use 1 */
+  uint32_t walk_ctas;       /* CTAs per SM of the persistent walk and tail grids (0: as many as fit, 1..32);
+                               fewer leave SMs to other requests that share the GPU */
 } gbpt_params;
 
 /* Renderer modes: the BDPT entries of the X-macro registry
@@ -211,6 +213,17 @@ gbpt_status gbpt_renderer_create(uint32_t width, uint32_t height, int32_t mode, 
                                  gbpt_renderer** out);
 gbpt_status gbpt_renderer_destroy(gbpt_renderer* r);
 gbpt_status gbpt_set_mode(gbpt_renderer* r, int32_t mode);
+/* No counterpart in the reference (one image per process there).  The
+ * renderer's width x height pixels become the window at (x0, y0) of a
+ * full_w x full_h image: camera rays are those of the full image's pixels and
+ * every path's random numbers follow from its full-image pixel id, so the
+ * windows of one image rendered apart (by separate renderers, processes or
+ * GPUs) reproduce the whole image's running means and sample counts to the
+ * bit.  (0, 0, width, height) is the whole image again.  Plain, filter-only
+ * (its unfiltered planes; the filter sees only the window) and PTSC modes;
+ * the adaptive modes, whose budget and filter couple every pixel, refuse a
+ * window with GBPT_ERR_STATE at render time.  Restarts accumulation. */
+gbpt_status gbpt_renderer_set_window(gbpt_renderer* r, uint32_t x0, uint32_t y0, uint32_t full_w, uint32_t full_h);
 gbpt_status gbpt_set_params(gbpt_renderer* r, const gbpt_params* params);
 gbpt_status gbpt_get_params(const gbpt_renderer* r, gbpt_params* params);
 /* RTRenderer::Render -> <codename>::Render(camPos, camDir, camUp, fov, scene,
@@ -422,7 +435,14 @@ gbpt_status gbpt_server_wait(gbpt_server* s, uint64_t id, uint32_t timeout_ms, g
 /* Forgets a finished request's status (a long-running server otherwise keeps
  * every status until it is destroyed); GBPT_ERR_STATE while it runs. */
 gbpt_status gbpt_server_release(gbpt_server* s, uint64_t id);
-/* The autotuner's choice for a class: *samples requests timed so far. */
+/* All knobs the autotuner holds for a request class: walk_refill, tail_from,
+ * bands and walk_ctas of *knobs (the other fields are the defaults); the
+ * class's first candidate when it has no samples yet; *samples requests
+ * timed so far. */
+gbpt_status gbpt_server_tuned_params(gbpt_server* s, int32_t mode, uint32_t depth, uint32_t width, uint32_t height,
+                                     gbpt_params* knobs, uint32_t* samples);
+/* The autotuner's choice for a class (its refill and tail knobs only):
+ * *samples requests timed so far. */
 gbpt_status gbpt_server_tuned(gbpt_server* s, int32_t mode, uint32_t depth, uint32_t width, uint32_t height,
                               uint32_t* walk_refill, int32_t* tail_from, uint32_t* samples);
 

@@ -383,3 +383,46 @@ def test_bands_change_no_pixel(gbdev, orc, mode):
                                                          render_iterations=3))
     ref.render(orc.Scene(v, t, m), cam, 4)
     assert_bits_equal(base[0], ref.get(0), "image against the oracle")
+
+
+@pytest.mark.parametrize("mode", [0, 3, 4])
+def test_windows_assemble_the_image(gbdev, mode):
+    """Windows of one image rendered by separate renderers (ragged row bands,
+    as cudapt_gb300.sharding assigns them, and 2x2 tiles) give the whole
+    image's running means and sample counts to the bit (the filter-only
+    mode's unfiltered planes)."""
+    from cudapt_gb300 import sharding
+    (v, t, m), cam = scene_arrays("interior")
+    s = gbdev.RTScene(v, t, m).build_bvh()
+    W, H, frames = 90, 71, 3
+    p = gbdev.default_params(eye_depth_max=10, light_depth_max=10, pt_depth_max=8, render_iterations=5)
+    full = gbdev.RTRenderer(W, H, mode, p)
+    for _ in range(frames):
+        full.render_frames(s, cam, 1, stats=False)
+    want_img, want_n = full.read_buffer(0), full.read_buffer(6)
+    full.close()
+    bands = [sharding.render_band(gbdev, s, cam, W, H, 3, k, frames, mode, p) for k in range(3)]
+    assert [b[1] for b in bands] == [24, 24, 23]
+    assert_bits_equal(sharding.assemble([b[2] for b in bands], W), want_img, "row bands")
+    assert_bits_equal(sharding.assemble([b[3] for b in bands], W, 1), want_n, "row-band sample counts")
+    img = np.zeros((H, W, 3), np.float32)
+    for x0, y0, w, h in ((0, 0, 45, 35), (45, 0, 45, 35), (0, 35, 45, 36), (45, 35, 45, 36)):
+        r = gbdev.RTRenderer(w, h, mode, p).set_window(x0, y0, W, H)
+        for _ in range(frames):
+            r.render_frames(s, cam, 1, stats=False)
+        img[y0:y0 + h, x0:x0 + w] = r.read_buffer(0).reshape(h, w, 3)
+        r.close()
+    assert_bits_equal(img.reshape(-1), want_img, "2x2 tiles")
+
+
+def test_window_refused_in_adaptive_mode(gbdev):
+    (v, t, m), cam = scene_arrays("cornell")
+    s = gbdev.RTScene(v, t, m).build_bvh()
+    r = gbdev.RTRenderer(16, 8, 1, gbdev.default_params()).set_window(0, 8, 16, 16)
+    with pytest.raises(gbdev.GbptError) as e:
+        r.render(s, cam)
+    assert e.value.status == 6
+    with pytest.raises(gbdev.GbptError):
+        r.set_window(4, 0, 16, 16)  # 16 columns do not fit from x = 4
+    r.set_window(0, 0, 16, 8)  # the whole image again
+    assert np.isfinite(r.render(s, cam)).all()

@@ -1,11 +1,12 @@
 """Row-band sharding of one image across ranks (world_size 2, gloo, CPU).
 
 Pixels are independent and every path's random numbers are fixed by its
-global pixel id, so each rank renders a band of rows and the gathered bands
-equal the single-process image bit for bit; the light-vertex cache is
-replicated (same key and frame on every rank) and the one global scalar of
-the adaptive mode (the error sum) is an all-reduce.  Runs the oracle: the
-pool's boxes carry one GPU, so the sharded path is exercised on host ranks.
+global pixel id, so each rank renders the band of rows that
+cudapt_gb300.sharding assigns it and the gathered bands equal the
+single-process image bit for bit; the light-vertex cache is replicated (same
+key and frame on every rank).  The ranks render with the oracle here (CPU
+ranks, no GPU); on a GPU the library renders the same bands through
+RTRenderer.set_window (tests/test_gpu_render.py::test_windows_assemble_the_image).
 """
 import os
 import socket
@@ -32,20 +33,25 @@ def _worker(rank, world, port, W, H, frames, out_dir):
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     import oracle
-    from cudapt_gb300 import layouts, scenes
+    from cudapt_gb300 import layouts, scenes, sharding
     (v, t, m), cam = scenes.cornell()
     sc = oracle.Scene(v, t, m)
-    rows = H // world
+    y0, rows = sharding.shard_rows(H, world, rank)
     r = oracle.Renderer(W, rows, 0, layouts.default_params(eye_depth_max=8, light_depth_max=8), threads=1)
-    r.set_window(0, rank * rows, W, H)
+    r.set_window(0, y0, W, H)
     r.render(sc, cam, frames)
     band = torch.from_numpy(r.get(0).copy())
-    bands = [torch.zeros_like(band) for _ in range(world)]
-    dist.all_gather(bands, band)
+    # ragged bands: gather padded to the largest, then cut each to its rows
+    most = sharding.shard_rows(H, world, 0)[1] * W * 3
+    padded = torch.zeros(most, dtype=band.dtype)
+    padded[: band.numel()] = band
+    bands = [torch.zeros_like(padded) for _ in range(world)]
+    dist.all_gather(bands, padded)
     total = band.double().sum()
     dist.all_reduce(total)
     if rank == 0:
-        np.save(os.path.join(out_dir, "img.npy"), torch.cat(bands).numpy())
+        parts = [bands[k][: sharding.shard_rows(H, world, k)[1] * W * 3].numpy() for k in range(world)]
+        np.save(os.path.join(out_dir, "img.npy"), sharding.assemble(parts, W))
         np.save(os.path.join(out_dir, "total.npy"), total.numpy())
     dist.barrier()
     dist.destroy_process_group()
@@ -53,7 +59,7 @@ def _worker(rank, world, port, W, H, frames, out_dir):
 
 def test_row_band_sharding_matches_single_rank(tmp_path, orc):
     import torch.multiprocessing as mp
-    W, H, frames = 32, 32, 3
+    W, H, frames = 32, 33, 3  # 33 rows: ragged bands (17 + 16)
     mp.spawn(_worker, args=(2, _free_port(), W, H, frames, str(tmp_path)), nprocs=2, join=True)
     img = np.load(tmp_path / "img.npy")
     from cudapt_gb300 import layouts, scenes
@@ -63,3 +69,15 @@ def test_row_band_sharding_matches_single_rank(tmp_path, orc):
     want = r.get(0)
     assert np.array_equal(img.view(np.uint32), want.view(np.uint32))
     assert abs(float(np.load(tmp_path / "total.npy")) - float(want.astype(np.float64).sum())) < 1e-6 * want.sum()
+
+
+def test_shard_rows_cover_the_image():
+    from cudapt_gb300 import sharding
+    for H in (1, 7, 33, 720):
+        for world in (1, 2, 3, 8):
+            parts = [sharding.shard_rows(H, world, k) for k in range(world)]
+            assert parts[0][0] == 0 and sum(r for _, r in parts) == H
+            assert all(parts[k][0] + parts[k][1] == parts[k + 1][0] for k in range(world - 1))
+            assert max(r for _, r in parts) - min(r for _, r in parts) <= 1
+    with pytest.raises(ValueError):
+        sharding.shard_rows(10, 2, 2)

@@ -64,13 +64,15 @@ def test_server_images_equal_single_renders(gbdev, policy, graphs):
 
 @pytest.mark.gpu
 def test_scheduling_knobs_change_no_pixel(gbdev):
-    """Refill threshold and the tail kernel's first bounce reorder work
-    between lanes only: every setting gives the same image."""
+    """Refill threshold, the tail kernel's first bounce and the persistent
+    grids' CTAs per SM reorder work between lanes only: every setting gives
+    the same image."""
     (v, t, m), cam = scene_arrays("interior")
     s = gbdev.RTScene(v, t, m).build_bvh()
     imgs = []
-    for refill, tail in ((0, -1), (12, -1), (28, 7), (20, 10), (5, 2)):
-        p = gbdev.default_params(eye_depth_max=10, light_depth_max=10, walk_refill=refill, tail_from=tail)
+    for refill, tail, ctas in ((0, -1, 0), (12, -1, 1), (28, 7, 2), (20, 10, 3), (5, 2, 0), (8, -1, 32)):
+        p = gbdev.default_params(eye_depth_max=10, light_depth_max=10, walk_refill=refill, tail_from=tail,
+                                 walk_ctas=ctas)
         imgs.append(_alone(gbdev, s, cam, 96, 72, 2, 0, p))
     for im in imgs[1:]:
         assert np.array_equal(im.view(np.uint32), imgs[0].view(np.uint32))
@@ -88,6 +90,9 @@ def test_server_autotuner_and_admission(gbdev):
         refill, tail, n = srv.tuned(0, 5, 64, 64)
         assert n == 16 and refill in (4, 8, 16) and tail in (-1, 2, 5)
         assert len({(r["walk_refill"], r["tail_from"]) for r in st}) >= 3  # candidates were explored
+        k = srv.tuned_knobs(0, 5, 64, 64)
+        assert k["samples"] == 16 and k["bands"] == 1 and k["walk_ctas"] in (0, 2, 3)
+        assert (k["walk_refill"], k["tail_from"]) == (refill, tail)
     # a released status is gone
     with serving.Server(workers=1) as srv:
         rid = srv.submit(s, cam, 32, 32, 1)

@@ -56,9 +56,11 @@ def adaptive_params(depth=5, **kw):
     return layouts.default_params(**base)
 
 
-def converged(gb, scene, cam, width, height, frames, depth=5):
-    """A long plain-BDPT render of the same estimator (the reference image)."""
-    r = gb.RTRenderer(width, height, layouts.MODE_BDPT_SC, adaptive_params(depth))
+def converged(gb, scene, cam, width, height, frames, depth=5, seed=1234):
+    """A long plain-BDPT render of the same estimator (the reference image);
+    `seed`: its Philox key (another key than the renders it scores shares no
+    samples with them)."""
+    r = gb.RTRenderer(width, height, layouts.MODE_BDPT_SC, adaptive_params(depth, seed=seed))
     for _ in range(frames - 1):
         r.render_frames(scene, cam, 1, stats=False)
     img = r.render(scene, cam, stats=False).copy()

@@ -351,6 +351,7 @@ struct gbpt_renderer {
     cacheEpoch[0] = cacheEpoch[1] = ~0ull;
     lightPending[0] = lightPending[1] = false;
     dfree(rb.ctr);
+    dfree(rb.carry);
     dfree(ab.err);
     dfree(ab.cnt);
     dfree(ab.off);
@@ -419,16 +420,21 @@ gbpt_status check_params(const gbpt_params* p) {
   if (p->tail_from < -1) return fail(GBPT_ERR_INVALID_ARG, "tail_from must be >= -1");
   if (p->bands > kMaxBands) return fail(GBPT_ERR_INVALID_ARG, "bands must be 0..8");
   if (p->walk_ctas > 32) return fail(GBPT_ERR_INVALID_ARG, "walk_ctas must be 0..32");
+  if (p->carry_steps > (1u << 20)) return fail(GBPT_ERR_INVALID_ARG, "carry_steps must be <= 2^20");
   return GBPT_OK;
 }
 
-// Bands of a frame: `requested` when set, else 2 from 512K camera paths.
-// Measured on GB300 (Mpaths/s, 1 / 2 / 3 / 4 bands): hall 1280x720 175.6 /
-// 180.9 / 176.4 / 165.3, interior 1024x768 154.7 / 157.4 / 144.8 / 137.1,
-// Cornell 256x256 206.3 / 188.6 (1 / 2).  A band's persistent walk holds its
-// SMs until its queue drains, so the bands of one frame stay nearly in step.
-uint32_t bands_for(uint32_t requested, size_t paths) {
+// Bands of a frame: `requested` when set, else 1 when the bounce launches
+// carry their last walks to the tail kernel (carrying removes the per-launch
+// wait that bands partly overlap, and the two together measured slower), else
+// 2 from 512K camera paths.  Measured on GB300 (Mpaths/s, 1 / 2 / 3 / 4
+// bands, no carrying): hall 1280x720 175.6 / 180.9 / 176.4 / 165.3, interior
+// 1024x768 154.7 / 157.4 / 144.8 / 137.1, Cornell 256x256 206.3 / 188.6 (1 / 2).
+// A band's persistent walk holds its SMs until its queue drains, so the bands
+// of one frame stay nearly in step.
+uint32_t bands_for(uint32_t requested, size_t paths, bool carrying) {
   if (requested) return std::min<uint32_t>(requested, kMaxBands);
+  if (carrying) return 1;
   return paths >= (1u << 19) ? 2u : 1u;
 }
 
@@ -451,6 +457,9 @@ RenderBuffers band_buffers(const RenderBuffers& rb, uint32_t b, uint32_t k, size
   x.sh[1] += 3 * p0;
   x.ctr = rb.ctr + b;
   x.lctr = rb.ctr;
+  const size_t c0 = (size_t)rb.carryCap * b / k, c1 = (size_t)rb.carryCap * (b + 1) / k;
+  x.carry = rb.carry + c0 * kCarryF4;
+  x.carryCap = (uint32_t)(c1 - c0);
   return x;
 }
 
@@ -459,7 +468,8 @@ RenderBuffers band_buffers(const RenderBuffers& rb, uint32_t b, uint32_t k, size
 uint64_t gbpt::renderer_bytes(uint32_t W, uint32_t H, const gbpt_params& p) {
   const size_t np = (size_t)W * H;
   const uint32_t cacheCap = std::max(1u, p.light_paths * (1 + p.light_depth_max));
-  return np * (128 + 16 + 96 + 16 + 48 + 16 + 8) + np * (12 * 10 + 4 * 2 + 4 * 5) + (size_t)cacheCap * 192;
+  return np * (128 + 16 + 96 + 16 + 48 + 16 + 8) + np * (12 * 10 + 4 * 2 + 4 * 5) + (size_t)cacheCap * 192 +
+         std::max<size_t>(np / 8, 256) * kCarryF4 * 16;
 }
 
 namespace {
@@ -491,6 +501,8 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   CK(dalloc(&r->rb.slotSmp, cap));
   CK(dalloc(&r->rb.cache[0], (size_t)cacheCap * 6));
   CK(dalloc(&r->rb.cache[1], (size_t)cacheCap * 6));
+  r->rb.carryCap = (uint32_t)std::max<size_t>(cap / 8, 256);
+  CK(dalloc(&r->rb.carry, (size_t)r->rb.carryCap * kCarryF4));
   CK(dalloc(&r->rb.ctr, kMaxBands));
   CK(cudaMemsetAsync(r->rb.ctr, 0, sizeof(DevCounters) * kMaxBands, r->st));
   r->rb.lctr = r->rb.ctr;
@@ -682,6 +694,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   a.tilesX = (r->W + 7) / 8;
   a.refill = r->p.walk_refill;
   a.walkCtas = r->p.walk_ctas;
+  a.carrySteps = r->p.carry_steps;
   if (a.moments && r->frame == 0)
     CK(cudaMemsetAsync(r->rb.hist, 0, (size_t)a.tilesX * ((r->H + 7) / 8) * 32, r->st));
   a.counting = r->counting ? 1u : 0u;
@@ -774,7 +787,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
     auto bounces = [&](const RenderBuffers& rbx, cudaStream_t sx, bool mk) -> gbpt_status {
       int in = 0;
       for (uint32_t d = 0; d < K; d++) {
-        CK(launch_walk(S, a, rbx, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), d == 1, sx));
+        CK(launch_walk(S, a, rbx, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), d == 1, d, sx));
         if (mk) mark(r, kPhTrace, tm);
         CK(launch_shade(S, a, rbx, in, d, K < D && d + 1 == K, sx));
         if (mk) mark(r, kPhShade, tm);
@@ -785,12 +798,14 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
       } else {
         // shadow rays of the last bounce (none in practice: paths at the depth cap
         // terminate without connecting; kept so the sequence needs no special case)
-        CK(launch_walk(S, a, rbx, -1, (int)((D - 1) & 1u), (int)(D & 1u), D == 1, sx));
+        CK(launch_walk(S, a, rbx, -1, (int)((D - 1) & 1u), (int)(D & 1u), D == 1, D, sx));
+        // the walks the bounce launches carried, and the rest of their paths
+        if (a.carrySteps && !(S.traversal == 1 && S.wide)) CK(launch_tail(S, a, rbx, -1, -1, D, sx));
       }
       return GBPT_OK;
     };
     const size_t np = (size_t)r->W * r->H;
-    const uint32_t nb = adaptive ? 1u : bands_for(r->p.bands, np);
+    const uint32_t nb = adaptive ? 1u : bands_for(r->p.bands, np, a.carrySteps && !(S.traversal == 1 && S.wide));
     r->lastBands = nb;
     if (budgeted || nb == 1) {
       if (!budgeted) {
@@ -1119,6 +1134,7 @@ gbpt_status gbpt_params_default(gbpt_params* p) {
   p->tail_from = -1;
   p->bands = 0;
   p->walk_ctas = 0;
+  p->carry_steps = 96;
   return GBPT_OK;
 }
 

@@ -289,6 +289,8 @@ __global__ void k_scan_blocks(uint32_t* blockSum, uint32_t nb, uint32_t gen, Dev
     ctr->wave[0] = (uint32_t)tot;
     ctr->paths = (uint32_t)tot;
     ctr->fetchT = 0;
+    ctr->carryN = 0;
+    ctr->fetchTail = 0;
   }
 }
 
@@ -734,6 +736,8 @@ __global__ void __launch_bounds__(256) k_bin_search(FrameArgs a, RenderBuffers b
     b.ctr->wave[0] = np;
     b.ctr->paths = np;
     b.ctr->fetchT = 0;
+    b.ctr->carryN = 0;
+    b.ctr->fetchTail = 0;
   }
 }
 

@@ -345,6 +345,8 @@ __global__ void k_camera(FrameArgs a, RenderBuffers b) {
     b.ctr->wave[0] = b.count;
     b.ctr->paths = b.count;
     b.ctr->fetchT = 0;
+    b.ctr->carryN = 0;
+    b.ctr->fetchTail = 0;
   }
   if (i >= b.count) return;
   const uint32_t p = b.base + i;
@@ -419,9 +421,42 @@ __host__ __device__ constexpr int walk_steps() {
   return kWide ? 2 : 6;
 }
 
+// One carried walk to the frame's carry buffer (out of line: it runs for a
+// few walks per launch, and keeping it out of the walk loop keeps that loop's
+// registers); false when the buffer is full.
+__device__ __noinline__ bool save_carry(const RenderBuffers& b, const Wave& wv, uint32_t item, uint32_t depth,
+                                        float minT, uint32_t best, float bu, float bv, float bw, uint32_t steps,
+                                        uint32_t tos, int sp, const uint32_t* stack) {
+  const uint32_t c = atomicAdd(&b.ctr->carryN, 1u);
+  if (c >= b.carryCap) return false;
+  float4* r = b.carry + (size_t)c * kCarryF4;
+  const float4 sm = wv.smp[item];
+  r[0] = wv.o[item];
+  r[1] = wv.d[item];
+  r[2] = wv.thr[item];
+  r[3] = make_float4(sm.x, sm.y, sm.z, __uint_as_float(depth));
+  r[4] = make_float4(minT, __uint_as_float(best), bu, bv);
+  r[5] = make_float4(bw, __uint_as_float(steps), __uint_as_float(tos), __int_as_float(sp));
+  for (int k = 0; k < 8; k++)
+    r[6 + k] = make_float4(__uint_as_float(stack[4 * k]), __uint_as_float(stack[4 * k + 1]),
+                           __uint_as_float(stack[4 * k + 2]), __uint_as_float(stack[4 * k + 3]));
+  b.hit[item] = make_float4(-2.f, 0.f, 0.f, 0.f);
+  return true;
+}
+
+// Carrying (reference order only): once the launch's ray queue is empty, a
+// warp keeps stepping its walks for carrySteps more steps; extension walks
+// still unfinished then are written, with their path, bounce and complete
+// walk state, to the frame's carry buffer, their hit word marked -2 (k_shade
+// skips them), and the frame's tail kernel resumes each at the step where it
+// stopped, then carries the path through its remaining bounces.  A path's
+// operations keep their order (its connection of the previous bounce was
+// walked in this launch, before its shading in the tail kernel), so results
+// are unchanged; the launch no longer waits for its few longest walks.
 template <bool kCount, bool kWide>
 __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, RenderBuffers b, int in, int shIn,
-                                                              int shReset, uint32_t shDirect, uint32_t kRefill) {
+                                                              int shReset, uint32_t shDirect, uint32_t kRefill,
+                                                              uint32_t depth, uint32_t carrySteps) {
   const uint32_t nE = (in >= 0) ? b.ctr->wave[in] : 0u;
   const uint32_t nS = (shIn >= 0) ? b.ctr->shadow[shIn] : 0u;
   const uint32_t n = nE + nS;
@@ -439,9 +474,18 @@ __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, Rend
   typename WalkOf<kWide>::Entry stack[WalkOf<kWide>::kDepth];
   bool has = false, drained = false, any = false;
   uint32_t item = 0, nnE = 0, ntE = 0, nnS = 0, ntS = 0;
+  uint32_t dryFor = 0;  // walk steps since this warp found the queue empty
   for (;;) {
     const uint32_t idle = __ballot_sync(0xffffffffu, !has);
     if (idle == 0xffffffffu && drained) break;
+    if constexpr (!kWide) {
+      if (carrySteps && drained && in >= 0) {
+        if (dryFor >= carrySteps && has && !any &&
+            save_carry(b, wv, item, depth, w.minT, w.best, w.bu, w.bv, w.bw, w.steps, w.tos, w.sp, stack))
+          has = false;
+        dryFor += walk_steps<kWide>();
+      }
+    }
     if (!drained && (idle == 0xffffffffu || __popc(idle) >= kRefill)) {
       const uint32_t cnt = __popc(idle);
       uint32_t base = 0;
@@ -637,11 +681,14 @@ __global__ void __launch_bounds__(kBlock, 3) k_shade(DevScene S, FrameArgs a, Re
     PathIO io;
     io.cont = io.conn = false;
     if (i < n) {
-      io.o = w.o[i];
-      io.d = w.d[i];
-      io.t = w.thr[i];
-      io.s = w.smp[i];
-      shade_path(S, a, b, cache, cacheSize, depth, b.hit[i], io);
+      const float4 h = b.hit[i];
+      if (h.x != -2.f) {  // -2: the walk was carried to the tail kernel, which shades it
+        io.o = w.o[i];
+        io.d = w.d[i];
+        io.t = w.thr[i];
+        io.s = w.smp[i];
+        shade_path(S, a, b, cache, cacheSize, depth, h, io);
+      }
     }
     const uint32_t mc = __ballot_sync(0xffffffffu, io.cont);
     if (mc) {
@@ -700,17 +747,19 @@ __host__ __device__ constexpr int tail_steps() { return 64; }
 template <bool kCount, bool kWide>
 __global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, RenderBuffers b, int in, int shIn,
                                                    uint32_t depth0, uint32_t kRefill) {
-  const uint32_t n = b.ctr->wave[in];
+  const uint32_t n = in >= 0 ? b.ctr->wave[in] : 0u;
+  const uint32_t nCarry = b.carry ? min(b.ctr->carryN, b.carryCap) : 0u;
+  const uint32_t total = n + nCarry;
   const uint32_t cacheSize = b.lctr->cacheSize[a.cacheSel];
   const float4* __restrict__ cache = b.cache[a.cacheSel];
   const float4* __restrict__ sh = b.sh[shIn >= 0 ? shIn : 0];
-  const Wave wv = b.wave[in];
+  const Wave wv = b.wave[in >= 0 ? in : 0];
   const uint32_t lane = threadIdx.x & 31;
   typename WalkOf<kWide>::type w;
   typename WalkOf<kWide>::Entry stack[WalkOf<kWide>::kDepth];
   PathIO io;
   uint32_t mode = kIdle, depth = 0;
-  bool drained = false;
+  bool drained = false, resumed = false;
   uint32_t extRays = 0, shRays = 0, nnE = 0, ntE = 0, nnS = 0, ntS = 0;
   for (;;) {
     const uint32_t idle = __ballot_sync(0xffffffffu, mode == kIdle);
@@ -718,12 +767,41 @@ __global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, Ren
     if (!drained && (idle == 0xffffffffu || __popc(idle) >= kRefill)) {
       const uint32_t cnt = __popc(idle);
       uint32_t base = 0;
-      if (lane == 0) base = atomicAdd(&b.ctr->fetchT, cnt);
+      if (lane == 0) base = atomicAdd(&b.ctr->fetchTail, cnt);
       base = __shfl_sync(0xffffffffu, base, 0);
-      if (base + cnt >= n) drained = true;
+      if (base + cnt >= total) drained = true;
       if (mode == kIdle) {
         const uint32_t j = base + __popc(idle & lanemask_lt());
-        if (j < n) {
+        if (j >= n && j < total) {  // a carried walk: resume it where it stopped
+          const float4* r = b.carry + (size_t)(j - n) * kCarryF4;
+          io.o = r[0];
+          io.d = r[1];
+          io.t = r[2];
+          io.s = r[3];
+          depth = __float_as_uint(r[3].w);
+          mode = kPathExt;
+          resumed = true;
+          w.init(ld3(io.o), ld3(io.d), gb::kInf, gb::kBias, stack);
+          if constexpr (!kWide) {
+            const float4 q = r[4], z = r[5];
+            w.minT = q.x;
+            w.best = __float_as_uint(q.y);
+            w.bu = q.z;
+            w.bv = q.w;
+            w.bw = z.x;
+            w.steps = __float_as_uint(z.y);
+            w.tos = __float_as_uint(z.z);
+            w.sp = __float_as_int(z.w);
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+              const float4 e = r[6 + k];
+              stack[4 * k] = __float_as_uint(e.x);
+              stack[4 * k + 1] = __float_as_uint(e.y);
+              stack[4 * k + 2] = __float_as_uint(e.z);
+              stack[4 * k + 3] = __float_as_uint(e.w);
+            }
+          }
+        } else if (j < n) {
           io.o = wv.o[j];
           io.d = wv.d[j];
           io.t = wv.thr[j];
@@ -765,8 +843,10 @@ __global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, Ren
       w.init(ld3(io.o), ld3(io.d), gb::kInf, gb::kBias, stack);
       continue;
     }
-    // closest hit of the path's current ray: shade it
-    extRays++;
+    // closest hit of the path's current ray: shade it (a resumed walk was
+    // counted by the bounce launch's shading kernel)
+    if (!resumed) extRays++;
+    resumed = false;
     const float4 h4 = w.hit() ? make_float4(w.minT, __uint_as_float(w.best), w.bu, w.bv)
                               : make_float4(-1.f, 0.f, 0.f, 0.f);
     shade_path(S, a, b, cache, cacheSize, depth, h4, io);
@@ -1022,9 +1102,9 @@ uint32_t persistent_grid(uint32_t full, uint32_t ctasPerSm) {
 
 template <bool kCount, bool kWide>
 void walk_variant(const DevScene& S, const RenderBuffers& b, int in, int shIn, int shReset, uint32_t sd,
-                  uint32_t refill, uint32_t ctas, cudaStream_t st) {
+                  uint32_t refill, uint32_t ctas, uint32_t depth, uint32_t carrySteps, cudaStream_t st) {
   const uint32_t g = persistent_grid(walk_grid<kCount, kWide>(), ctas);
-  k_walk<kCount, kWide><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, sd, refill);
+  k_walk<kCount, kWide><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, sd, refill, depth, carrySteps);
 }
 
 template <bool kCount, bool kWide>
@@ -1035,16 +1115,17 @@ void tail_variant(const DevScene& S, const FrameArgs& a, const RenderBuffers& b,
 }
 
 cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
-                        int shReset, bool shDirect, cudaStream_t st) {
+                        int shReset, bool shDirect, uint32_t depth, cudaStream_t st) {
   const uint32_t sd = (a.bilat && shDirect) ? 1u : 0u;
   const bool wide = S.traversal == 1 && S.wide;
   const uint32_t rf = walk_refill_for(a.refill, wide);
+  const uint32_t cs = b.carry ? a.carrySteps : 0u;
   if (a.counting) {
-    if (wide) walk_variant<true, true>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, st);
-    else walk_variant<true, false>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, st);
+    if (wide) walk_variant<true, true>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, depth, 0u, st);
+    else walk_variant<true, false>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, depth, cs, st);
   } else {
-    if (wide) walk_variant<false, true>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, st);
-    else walk_variant<false, false>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, st);
+    if (wide) walk_variant<false, true>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, depth, 0u, st);
+    else walk_variant<false, false>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, depth, cs, st);
   }
   note_launches(1);
   return cudaGetLastError();

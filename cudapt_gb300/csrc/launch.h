@@ -56,6 +56,8 @@ struct DevCounters {
   unsigned long long rays, nodes, tris;  // cumulative work counters (closest-hit walks)
   unsigned long long shadowRays, nodesS, trisS;  // any-hit (shadow) walks
   double errSum;          // adaptive: sum of per-pixel errors
+  uint32_t carryN;        // extension walks handed from the bounce launches to the tail kernel this frame
+  uint32_t fetchTail;     // next item handed to a lane by the tail kernel
 };
 
 // Path state of one wavefront (structure of arrays, float4-packed).
@@ -89,6 +91,10 @@ struct FrameArgs {
   // W and H above are the full image's for the camera projection, width and
   // height the window's
   uint32_t winX0, winY0, fullW;
+  // walk steps a warp keeps stepping its extension walks after the launch's
+  // ray queue ran dry before it carries the unfinished ones to the tail kernel
+  // (0: never; the reference-order walk only)
+  uint32_t carrySteps;
 };
 
 struct RenderBuffers {
@@ -116,8 +122,15 @@ struct RenderBuffers {
   // the renderer's buffers, and per-slot arrays stay indexed by pixel.
   uint32_t base;
   uint32_t count;
+  // extension walks still running when a bounce launch's other work is done
+  // are handed over (carried) to the frame's tail kernel instead of being
+  // waited for: kCarryF4 float4 per walk (the path, its depth, the walk's state
+  // and stack), up to carryCap walks per frame and band
+  float4* carry;
+  uint32_t carryCap;
 };
 constexpr uint32_t kMaxBands = 8;
+constexpr uint32_t kCarryF4 = 14;
 
 // wavefront kernels (kernels_wave.cu)
 cudaError_t launch_light_pass(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, cudaStream_t st);
@@ -127,13 +140,15 @@ cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream
 // resets the counters of wave in^1 and of connection queue `shReset`
 // (shDirect: the connection queue holds bounce-0 connections, which update
 // the direct-light sample of the filter-only mode)
+// (depth: the bounce of wave `in`'s extension rays, recorded with a carried walk)
 cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
-                        int shReset, bool shDirect, cudaStream_t st);
+                        int shReset, bool shDirect, uint32_t depth, cudaStream_t st);
 // attach: store each continuing path's connection at the path's index (for the tail kernel)
 cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t depth,
                          bool attach, cudaStream_t st);
-// remaining bounces of every path of wave `in` (at bounce depth0), starting
-// with the connection attached to it in queue shIn; one lane per path
+// remaining bounces of every path of wave `in` (at bounce depth0; in < 0: no
+// wave), starting with the connection attached to it in queue shIn, then of
+// every walk the bounce launches carried; one lane per path
 cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
                         uint32_t depth0, cudaStream_t st);
 // first bounce handled by the tail kernel: `requested` when >= 0 (>= D: none),

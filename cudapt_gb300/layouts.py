@@ -69,6 +69,7 @@ PARAMS = np.dtype(
         ("tail_from", "<i4"),
         ("bands", "<u4"),
         ("walk_ctas", "<u4"),
+        ("carry_steps", "<u4"),
     ]
 )
 
@@ -122,6 +123,7 @@ def default_params(**over):
     p["tail_from"] = -1
     p["bands"] = 0
     p["walk_ctas"] = 0
+    p["carry_steps"] = 96
     for k, v in over.items():
         p[k] = v
     return p

@@ -106,9 +106,13 @@ typedef struct gbpt_params {
   int32_t tail_from;        /* first bounce the per-path tail kernel carries (>= the depth cap: none;
                                -1: depth / 2 - 1 (wide order: depth / 2) when the cap exceeds 6, else none) */
   uint32_t bands;           /* wavefronts a frame's camera paths are split into, each on its own stream
-                               (1..8; 0: 2 from 512K paths, else 1); the adaptive modes use 1 */
+                               (1..8; 0: 1 while carry_steps is on, else 2 from 512K paths, else 1); the
+                               adaptive modes use 1 */
   uint32_t walk_ctas;       /* CTAs per SM of the persistent walk and tail grids (0: as many as fit, 1..32);
                                fewer leave SMs to other requests that share the GPU */
+  uint32_t carry_steps;     /* walk steps a bounce launch keeps stepping its last extension walks after
+                               its ray queue ran dry before handing the unfinished ones, mid-walk, to the
+                               frame's tail kernel (0: never; default 96; the reference-order walk only) */
 } gbpt_params;
 
 /* Renderer modes: the BDPT entries of the X-macro registry

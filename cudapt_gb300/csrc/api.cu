@@ -351,7 +351,8 @@ struct gbpt_renderer {
     cacheEpoch[0] = cacheEpoch[1] = ~0ull;
     lightPending[0] = lightPending[1] = false;
     dfree(rb.ctr);
-    dfree(rb.carry);
+    dfree(rb.carry[0]);
+    dfree(rb.carry[1]);
     dfree(ab.err);
     dfree(ab.cnt);
     dfree(ab.off);
@@ -421,17 +422,19 @@ gbpt_status check_params(const gbpt_params* p) {
   if (p->bands > kMaxBands) return fail(GBPT_ERR_INVALID_ARG, "bands must be 0..8");
   if (p->walk_ctas > 32) return fail(GBPT_ERR_INVALID_ARG, "walk_ctas must be 0..32");
   if (p->carry_steps > (1u << 20)) return fail(GBPT_ERR_INVALID_ARG, "carry_steps must be <= 2^20");
+  if (!(p->tail_below >= 0.f && p->tail_below <= 1.f))
+    return fail(GBPT_ERR_INVALID_ARG, "tail_below must be in [0, 1]");
   return GBPT_OK;
 }
 
 // Bands of a frame: `requested` when set, else 1 when the bounce launches
-// carry their last walks to the tail kernel (carrying removes the per-launch
-// wait that bands partly overlap, and the two together measured slower), else
-// 2 from 512K camera paths.  Measured on GB300 (Mpaths/s, 1 / 2 / 3 / 4
-// bands, no carrying): hall 1280x720 175.6 / 180.9 / 176.4 / 165.3, interior
-// 1024x768 154.7 / 157.4 / 144.8 / 137.1, Cornell 256x256 206.3 / 188.6 (1 / 2).
-// A band's persistent walk holds its SMs until its queue drains, so the bands
-// of one frame stay nearly in step.
+// carry their last walks on (carrying removes the per-launch wait that bands
+// partly overlap; carrying with 2 bands measured 127-164 against 173 Mpaths/s
+// with 1 on the hall), else 2 from 512K camera paths.  Measured on GB300
+// (Mpaths/s, 1 / 2 / 3 / 4 bands, no carrying): hall 1280x720 175.6 / 180.9 /
+// 176.4 / 165.3, interior 1024x768 154.7 / 157.4 / 144.8 / 137.1, Cornell
+// 256x256 206.3 / 188.6 (1 / 2).  A band's persistent walk holds its SMs
+// until its queue drains, so the bands of one frame stay nearly in step.
 uint32_t bands_for(uint32_t requested, size_t paths, bool carrying) {
   if (requested) return std::min<uint32_t>(requested, kMaxBands);
   if (carrying) return 1;
@@ -458,7 +461,8 @@ RenderBuffers band_buffers(const RenderBuffers& rb, uint32_t b, uint32_t k, size
   x.ctr = rb.ctr + b;
   x.lctr = rb.ctr;
   const size_t c0 = (size_t)rb.carryCap * b / k, c1 = (size_t)rb.carryCap * (b + 1) / k;
-  x.carry = rb.carry + c0 * kCarryF4;
+  x.carry[0] = rb.carry[0] + c0 * kCarryF4;
+  x.carry[1] = rb.carry[1] + c0 * kCarryF4;
   x.carryCap = (uint32_t)(c1 - c0);
   return x;
 }
@@ -469,7 +473,7 @@ uint64_t gbpt::renderer_bytes(uint32_t W, uint32_t H, const gbpt_params& p) {
   const size_t np = (size_t)W * H;
   const uint32_t cacheCap = std::max(1u, p.light_paths * (1 + p.light_depth_max));
   return np * (128 + 16 + 96 + 16 + 48 + 16 + 8) + np * (12 * 10 + 4 * 2 + 4 * 5) + (size_t)cacheCap * 192 +
-         std::max<size_t>(np / 8, 256) * kCarryF4 * 16;
+         2 * std::max<size_t>(np / 8, 256) * kCarryF4 * 16;
 }
 
 namespace {
@@ -502,7 +506,8 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   CK(dalloc(&r->rb.cache[0], (size_t)cacheCap * 6));
   CK(dalloc(&r->rb.cache[1], (size_t)cacheCap * 6));
   r->rb.carryCap = (uint32_t)std::max<size_t>(cap / 8, 256);
-  CK(dalloc(&r->rb.carry, (size_t)r->rb.carryCap * kCarryF4));
+  CK(dalloc(&r->rb.carry[0], (size_t)r->rb.carryCap * kCarryF4));
+  CK(dalloc(&r->rb.carry[1], (size_t)r->rb.carryCap * kCarryF4));
   CK(dalloc(&r->rb.ctr, kMaxBands));
   CK(cudaMemsetAsync(r->rb.ctr, 0, sizeof(DevCounters) * kMaxBands, r->st));
   r->rb.lctr = r->rb.ctr;
@@ -695,6 +700,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
   a.refill = r->p.walk_refill;
   a.walkCtas = r->p.walk_ctas;
   a.carrySteps = r->p.carry_steps;
+  a.tailBelow = r->p.tail_below;
   if (a.moments && r->frame == 0)
     CK(cudaMemsetAsync(r->rb.hist, 0, (size_t)a.tilesX * ((r->H + 7) / 8) * 32, r->st));
   a.counting = r->counting ? 1u : 0u;
@@ -778,34 +784,38 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
         CK(launch_adapt_budget(a, r->rb, r->ab, r->result, r->sampleN, r->p.desired_n, st));
       mark(r, kPhAdapt, tm);
     }
-    // bounce d < K: walk (extension rays of d + shadow rays of d-1), then shade
-    // d, one launch each; bounces >= K: one persistent kernel per frame carries
-    // every remaining path to its end (few paths are left by then, and per-bounce
-    // launches would each wait for their slowest ray)
+    // bounce launch d < K: walk (the walks launch d - 1 carried, the extension
+    // rays of its wave, the shadow rays of launch d - 1), then shade, one launch
+    // each; from K (or the bounce a shading launch switched at): one persistent
+    // kernel per frame carries every remaining path to its end (few paths are
+    // left by then, and per-bounce launches would each wait for their slowest
+    // ray).  Without carrying or a switch on the device and with K = D, the
+    // last launch walks the final connections instead of the tail kernel.
     const uint32_t D = a.eyeDepth;
-    const uint32_t K = std::min(tail_from(D, S.traversal == 1 && S.wide, r->p.tail_from), D);
+    const bool wideT = S.traversal == 1 && S.wide;
+    const uint32_t K = std::min(tail_from(D, wideT, r->p.tail_from), D);
+    const bool carrying = a.carrySteps && !wideT;
+    const bool tailRun = K < D || carrying || a.tailBelow > 0.f;
     auto bounces = [&](const RenderBuffers& rbx, cudaStream_t sx, bool mk) -> gbpt_status {
       int in = 0;
       for (uint32_t d = 0; d < K; d++) {
-        CK(launch_walk(S, a, rbx, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), d == 1, d, sx));
+        CK(launch_walk(S, a, rbx, in, d > 0 ? (int)((d - 1) & 1u) : -1, (int)(d & 1u), d, sx));
         if (mk) mark(r, kPhTrace, tm);
-        CK(launch_shade(S, a, rbx, in, d, K < D && d + 1 == K, sx));
+        CK(launch_shade(S, a, rbx, in, d, tailRun && d + 1 == K, sx));
         if (mk) mark(r, kPhShade, tm);
         in ^= 1;
       }
-      if (K < D) {
-        CK(launch_tail(S, a, rbx, in, K > 0 ? (int)((K - 1) & 1u) : -1, K, sx));
+      if (tailRun) {
+        CK(launch_tail(S, a, rbx, K, sx));
       } else {
         // shadow rays of the last bounce (none in practice: paths at the depth cap
         // terminate without connecting; kept so the sequence needs no special case)
-        CK(launch_walk(S, a, rbx, -1, (int)((D - 1) & 1u), (int)(D & 1u), D == 1, D, sx));
-        // the walks the bounce launches carried, and the rest of their paths
-        if (a.carrySteps && !(S.traversal == 1 && S.wide)) CK(launch_tail(S, a, rbx, -1, -1, D, sx));
+        CK(launch_walk(S, a, rbx, -1, (int)((D - 1) & 1u), (int)(D & 1u), D, sx));
       }
       return GBPT_OK;
     };
     const size_t np = (size_t)r->W * r->H;
-    const uint32_t nb = adaptive ? 1u : bands_for(r->p.bands, np, a.carrySteps && !(S.traversal == 1 && S.wide));
+    const uint32_t nb = adaptive ? 1u : bands_for(r->p.bands, np, carrying);
     r->lastBands = nb;
     if (budgeted || nb == 1) {
       if (!budgeted) {
@@ -1134,7 +1144,8 @@ gbpt_status gbpt_params_default(gbpt_params* p) {
   p->tail_from = -1;
   p->bands = 0;
   p->walk_ctas = 0;
-  p->carry_steps = 96;
+  p->carry_steps = 64;
+  p->tail_below = 0.f;
   return GBPT_OK;
 }
 

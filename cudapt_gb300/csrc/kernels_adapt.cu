@@ -289,8 +289,9 @@ __global__ void k_scan_blocks(uint32_t* blockSum, uint32_t nb, uint32_t gen, Dev
     ctr->wave[0] = (uint32_t)tot;
     ctr->paths = (uint32_t)tot;
     ctr->fetchT = 0;
-    ctr->carryN = 0;
+    ctr->carryN[0] = ctr->carryN[1] = ctr->carryN[2] = 0;
     ctr->fetchTail = 0;
+    ctr->tailAt = 0xFFFFFFFFu;
   }
 }
 
@@ -736,8 +737,9 @@ __global__ void __launch_bounds__(256) k_bin_search(FrameArgs a, RenderBuffers b
     b.ctr->wave[0] = np;
     b.ctr->paths = np;
     b.ctr->fetchT = 0;
-    b.ctr->carryN = 0;
+    b.ctr->carryN[0] = b.ctr->carryN[1] = b.ctr->carryN[2] = 0;
     b.ctr->fetchTail = 0;
+    b.ctr->tailAt = 0xFFFFFFFFu;
   }
 }
 

@@ -345,8 +345,9 @@ __global__ void k_camera(FrameArgs a, RenderBuffers b) {
     b.ctr->wave[0] = b.count;
     b.ctr->paths = b.count;
     b.ctr->fetchT = 0;
-    b.ctr->carryN = 0;
+    b.ctr->carryN[0] = b.ctr->carryN[1] = b.ctr->carryN[2] = 0;
     b.ctr->fetchTail = 0;
+    b.ctr->tailAt = 0xFFFFFFFFu;
   }
   if (i >= b.count) return;
   const uint32_t p = b.base + i;
@@ -421,58 +422,94 @@ __host__ __device__ constexpr int walk_steps() {
   return kWide ? 2 : 6;
 }
 
-// One carried walk to the frame's carry buffer (out of line: it runs for a
-// few walks per launch, and keeping it out of the walk loop keeps that loop's
-// registers); false when the buffer is full.
-__device__ __noinline__ bool save_carry(const RenderBuffers& b, const Wave& wv, uint32_t item, uint32_t depth,
-                                        float minT, uint32_t best, float bu, float bv, float bw, uint32_t steps,
-                                        uint32_t tos, int sp, const uint32_t* stack) {
-  const uint32_t c = atomicAdd(&b.ctr->carryN, 1u);
-  if (c >= b.carryCap) return false;
-  float4* r = b.carry + (size_t)c * kCarryF4;
-  const float4 sm = wv.smp[item];
-  r[0] = wv.o[item];
-  r[1] = wv.d[item];
-  r[2] = wv.thr[item];
-  r[3] = make_float4(sm.x, sm.y, sm.z, __uint_as_float(depth));
+// One carried walk to carry buffer `dst` (out of line: it runs for a few
+// walks per launch, and keeping it out of the walk loop keeps that loop's
+// registers): the path (po..ps, its depth in ps.w), the walk's state and its
+// node stack; false when the buffer is full.
+__device__ __noinline__ bool save_carry(float4* dst, uint32_t* cnt, uint32_t cap, const float4* po,
+                                        const float4* pd, const float4* pt, const float4* ps, float minT,
+                                        uint32_t best, float bu, float bv, float bw, uint32_t steps, uint32_t tos,
+                                        int sp, const uint32_t* stack) {
+  const uint32_t c = atomicAdd(cnt, 1u);
+  if (c >= cap) return false;
+  float4* r = dst + (size_t)c * kCarryF4;
+  r[0] = *po;
+  r[1] = *pd;
+  r[2] = *pt;
+  r[3] = *ps;
   r[4] = make_float4(minT, __uint_as_float(best), bu, bv);
   r[5] = make_float4(bw, __uint_as_float(steps), __uint_as_float(tos), __int_as_float(sp));
   for (int k = 0; k < 8; k++)
     r[6 + k] = make_float4(__uint_as_float(stack[4 * k]), __uint_as_float(stack[4 * k + 1]),
                            __uint_as_float(stack[4 * k + 2]), __uint_as_float(stack[4 * k + 3]));
-  b.hit[item] = make_float4(-2.f, 0.f, 0.f, 0.f);
   return true;
+}
+
+// The walk of carry record r, resumed at the step where it stopped.
+__device__ __forceinline__ void resume_walk(const float4* r, Walk& w, uint32_t* stack) {
+  w.init(ld3(r[0]), ld3(r[1]), gb::kInf, gb::kBias, stack);
+  const float4 q = r[4], z = r[5];
+  w.minT = q.x;
+  w.best = __float_as_uint(q.y);
+  w.bu = q.z;
+  w.bv = q.w;
+  w.bw = z.x;
+  w.steps = __float_as_uint(z.y);
+  w.tos = __float_as_uint(z.z);
+  w.sp = __float_as_int(z.w);
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const float4 e = r[6 + k];
+    stack[4 * k] = __float_as_uint(e.x);
+    stack[4 * k + 1] = __float_as_uint(e.y);
+    stack[4 * k + 2] = __float_as_uint(e.z);
+    stack[4 * k + 3] = __float_as_uint(e.w);
+  }
+}
+
+// walks carried out of bounce launch L (buffer L & 1, counter L % 3; the
+// counter of launch L + 1 is reset by launch L, after its last reader)
+__device__ __forceinline__ uint32_t carried_of(const RenderBuffers& b, uint32_t launch) {
+  return b.carry[0] ? min(b.ctr->carryN[launch % 3u], b.carryCap) : 0u;
 }
 
 // Carrying (reference order only): once the launch's ray queue is empty, a
 // warp keeps stepping its walks for carrySteps more steps; extension walks
-// still unfinished then are written, with their path, bounce and complete
-// walk state, to the frame's carry buffer, their hit word marked -2 (k_shade
-// skips them), and the frame's tail kernel resumes each at the step where it
-// stopped, then carries the path through its remaining bounces.  A path's
+// still unfinished then are written, with their path and complete walk
+// state, to the launch's carry buffer and their hit word marked -2 (k_shade
+// skips them).  The next bounce launch resumes them first (items 0 .. nC-1,
+// their hits stored after its own extension rays' at nE + k) and its shading
+// kernel shades them at their own depth, one bounce behind the paths around
+// them; the tail kernel takes those of the last bounce launch.  A path's
 // operations keep their order (its connection of the previous bounce was
-// walked in this launch, before its shading in the tail kernel), so results
-// are unchanged; the launch no longer waits for its few longest walks.
+// walked before it was carried; every random number is keyed by the path's
+// own depth), so results are unchanged; a launch no longer waits for its few
+// longest walks.
 template <bool kCount, bool kWide>
 __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, RenderBuffers b, int in, int shIn,
-                                                              int shReset, uint32_t shDirect, uint32_t kRefill,
-                                                              uint32_t depth, uint32_t carrySteps) {
+                                                              int shReset, uint32_t bilat, uint32_t kRefill,
+                                                              uint32_t launch, uint32_t carrySteps) {
+  if (b.ctr->tailAt <= launch) return;  // the frame's tail kernel carries this bounce
+  const uint32_t nC = (!kWide && in >= 0 && launch > 0) ? carried_of(b, launch - 1) : 0u;
   const uint32_t nE = (in >= 0) ? b.ctr->wave[in] : 0u;
   const uint32_t nS = (shIn >= 0) ? b.ctr->shadow[shIn] : 0u;
-  const uint32_t n = nE + nS;
+  const uint32_t nCE = nC + nE;
+  const uint32_t n = nCE + nS;
   uint32_t* fetch = &b.ctr->fetchT;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     atomicAdd(&b.ctr->rays, (unsigned long long)nS);
     atomicAdd(&b.ctr->shadowRays, (unsigned long long)nS);
     if (in >= 0) b.ctr->wave[in ^ 1] = 0;
     b.ctr->shadow[shReset] = 0;
+    b.ctr->carryN[(launch + 1) % 3u] = 0;
   }
   const Wave wv = b.wave[in >= 0 ? in : 0];
   const float4* __restrict__ sh = b.sh[shIn >= 0 ? shIn : 0];
+  const float4* prev = b.carry[(launch + 1) & 1u];  // launch - 1's carried walks
   const uint32_t lane = threadIdx.x & 31;
   typename WalkOf<kWide>::type w;
   typename WalkOf<kWide>::Entry stack[WalkOf<kWide>::kDepth];
-  bool has = false, drained = false, any = false;
+  bool has = false, drained = false, any = false, res = false;
   uint32_t item = 0, nnE = 0, ntE = 0, nnS = 0, ntS = 0;
   uint32_t dryFor = 0;  // walk steps since this warp found the queue empty
   for (;;) {
@@ -480,9 +517,19 @@ __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, Rend
     if (idle == 0xffffffffu && drained) break;
     if constexpr (!kWide) {
       if (carrySteps && drained && in >= 0) {
-        if (dryFor >= carrySteps && has && !any &&
-            save_carry(b, wv, item, depth, w.minT, w.best, w.bu, w.bv, w.bw, w.steps, w.tos, w.sp, stack))
-          has = false;
+        if (dryFor >= carrySteps && has && !any) {
+          const float4* r = prev + (size_t)item * kCarryF4;
+          const bool saved = res ? save_carry(b.carry[launch & 1u], &b.ctr->carryN[launch % 3u], b.carryCap, r,
+                                              r + 1, r + 2, r + 3, w.minT, w.best, w.bu, w.bv, w.bw, w.steps, w.tos,
+                                              w.sp, stack)
+                                 : save_carry(b.carry[launch & 1u], &b.ctr->carryN[launch % 3u], b.carryCap,
+                                              wv.o + item, wv.d + item, wv.thr + item, wv.smp + item, w.minT, w.best,
+                                              w.bu, w.bv, w.bw, w.steps, w.tos, w.sp, stack);
+          if (saved) {
+            b.hit[res ? nE + item : item] = make_float4(-2.f, 0.f, 0.f, 0.f);
+            has = false;
+          }
+        }
         dryFor += walk_steps<kWide>();
       }
     }
@@ -496,11 +543,14 @@ __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, Rend
         const uint32_t k = base + __popc(idle & lanemask_lt());
         if (k < n) {
           has = true;
-          any = k >= nE;
-          item = any ? k - nE : k;
+          any = k >= nCE;
+          res = k < nC;
+          item = any ? k - nCE : (res ? k : k - nC);
           if (any) {
             const float4 A = sh[3 * (size_t)item], B = sh[3 * (size_t)item + 1];
             w.init(ld3(A), ld3(B), B.w, gb::kBias, stack);
+          } else if (res) {
+            if constexpr (!kWide) resume_walk(prev + (size_t)item * kCarryF4, w, stack);
           } else {
             w.init(ld3(wv.o[item]), ld3(wv.d[item]), gb::kInf, gb::kBias, stack);
           }
@@ -530,11 +580,11 @@ __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, Rend
             const float4 r = b.res[slot];
             b.res[slot] =
                 make_float4(r.x + C.x, r.y + C.y, r.z + C.z, __uint_as_float(__float_as_uint(r.w) + 4u));
-            if (shDirect) direct_connect(b.dsm, slot, C);
+            if (bilat && __float_as_uint(C.w) == 0u) direct_connect(b.dsm, slot, C);  // made at bounce 0
           }
         } else {
-          b.hit[item] = w.hit() ? make_float4(w.minT, __uint_as_float(w.best), w.bu, w.bv)
-                                : make_float4(-1.f, 0.f, 0.f, 0.f);
+          b.hit[res ? nE + item : item] = w.hit() ? make_float4(w.minT, __uint_as_float(w.best), w.bu, w.bv)
+                                                  : make_float4(-1.f, 0.f, 0.f, 0.f);
         }
       }
     }
@@ -626,7 +676,7 @@ __device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a
   io.o = st4u(B.nOrig, slot);
   io.d = st4u(B.nDir, pix);
   io.t = st4(outMul, pot);
-  io.s = st4(pathSample, 0.f);
+  io.s = make_float4(pathSample.x, pathSample.y, pathSample.z, __uint_as_float(depth + 1));
   if (B.type != kTypeDiff || cacheSize == 0 || a.ptsc) return;
   // connection: pick a cached light vertex, shade both ends (:665-723)
   f3 pos = B.nOrig + B.nl * kBias;
@@ -650,44 +700,65 @@ __device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a
     io.conn = true;
     io.shA = st4u(pos, slot);
     io.shB = st4(toDir, toDist - kBias);
-    io.shC = st4(vmul(c, inMul), 0.f);
+    const f3 cw = vmul(c, inMul);
+    io.shC = make_float4(cw.x, cw.y, cw.z, __uint_as_float(depth));  // .w: the bounce that made it
   }
 }
 
-// Shading of one wave; survivors are appended to the other wave buffer and
-// connection requests to queue depth & 1, one atomic per warp each.
-// attach != 0 (the last bounce before the tail kernel): each continuing
+// Shading of bounce launch L: the paths of its wave, then the walks it
+// resumed for launch L - 1 (carry records, their hits after the wave's), each
+// at its own depth; survivors are appended to the other wave buffer and
+// connection requests to queue L & 1, one atomic per warp each.
+// attach != 0 (the last bounce launch before the tail kernel): each continuing
 // path's connection record is stored at the path's own index j of queue
-// depth & 1 (slot word 0xffffffff when it has none), so that the tail kernel
+// L & 1 (slot word 0xffffffff when it has none), so that the tail kernel
 // walks it on the path's lane before the path's next bounce.  Three CTAs per
 // SM (80 registers, a few bytes of spill) beat two at 96 registers: shading
 // time -10 to -12% on the interior and hall walks.
-__global__ void __launch_bounds__(kBlock, 3) k_shade(DevScene S, FrameArgs a, RenderBuffers b, int in, uint32_t depth,
+__global__ void __launch_bounds__(kBlock, 3) k_shade(DevScene S, FrameArgs a, RenderBuffers b, int in, uint32_t launch,
                                                      uint32_t attach) {
+  if (b.ctr->tailAt <= launch) return;  // the frame's tail kernel carries this bounce
   const uint32_t n = b.ctr->wave[in];
+  const uint32_t nC = launch > 0 ? carried_of(b, launch - 1) : 0u;
+  const uint32_t total = n + nC;
+  // the switch decided on the device: with fewer than tailBelow x the band's
+  // camera paths alive at this launch, the paths that continue go to the tail
+  // kernel from the next launch (every CTA reads the same counts and decides alike)
+  if (!attach && a.tailBelow > 0.f && launch + 1 < a.eyeDepth && (float)total < a.tailBelow * (float)b.ctr->paths)
+    attach = 2u;
   const uint32_t cacheSize = b.lctr->cacheSize[a.cacheSel];
   const float4* __restrict__ cache = b.cache[a.cacheSel];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    atomicAdd(&b.ctr->rays, (unsigned long long)n);
+    atomicAdd(&b.ctr->rays, (unsigned long long)n);  // resumed walks were counted by their own launch
     b.ctr->fetchT = 0;  // for the next walk (next bounce's rays + this bounce's shadow rays)
+    if (attach == 2u) b.ctr->tailAt = launch + 1;
   }
   const Wave w = b.wave[in];
   const Wave wo = b.wave[in ^ 1];
+  const float4* prev = b.carry[(launch + 1) & 1u];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t lane = threadIdx.x & 31;
-  float4* shq = b.sh[depth & 1u];
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+  float4* shq = b.sh[launch & 1u];
+  for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += stride) {
     const uint32_t i = base + threadIdx.x;
     PathIO io;
     io.cont = io.conn = false;
-    if (i < n) {
+    if (i < total) {
       const float4 h = b.hit[i];
-      if (h.x != -2.f) {  // -2: the walk was carried to the tail kernel, which shades it
-        io.o = w.o[i];
-        io.d = w.d[i];
-        io.t = w.thr[i];
-        io.s = w.smp[i];
-        shade_path(S, a, b, cache, cacheSize, depth, h, io);
+      if (h.x != -2.f) {  // -2: the walk was carried on, to the next launch or the tail kernel
+        if (i < n) {
+          io.o = w.o[i];
+          io.d = w.d[i];
+          io.t = w.thr[i];
+          io.s = w.smp[i];
+        } else {
+          const float4* r = prev + (size_t)(i - n) * kCarryF4;
+          io.o = r[0];
+          io.d = r[1];
+          io.t = r[2];
+          io.s = r[3];
+        }
+        shade_path(S, a, b, cache, cacheSize, __float_as_uint(io.s.w), h, io);
       }
     }
     const uint32_t mc = __ballot_sync(0xffffffffu, io.cont);
@@ -712,7 +783,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_shade(DevScene S, FrameArgs a, Re
     const uint32_t ms = __ballot_sync(0xffffffffu, io.conn);
     if (ms) {
       uint32_t basej = 0;
-      if (lane == 0) basej = atomicAdd(&b.ctr->shadow[depth & 1u], __popc(ms));
+      if (lane == 0) basej = atomicAdd(&b.ctr->shadow[launch & 1u], __popc(ms));
       basej = __shfl_sync(0xffffffffu, basej, 0);
       if (io.conn) {
         const uint32_t j = basej + __popc(ms & lanemask_lt());
@@ -727,12 +798,14 @@ __global__ void __launch_bounds__(kBlock, 3) k_shade(DevScene S, FrameArgs a, Re
 // ---------------------------------------------------------------------------
 // Tail of a frame: once few paths are left, per-bounce launches are bounded
 // by their slowest ray.  This persistent kernel instead carries every path
-// of wave `in` (at bounce depth0) through all its remaining bounces on one
-// lane: the connection attached to it by the previous bounce (queue shIn,
-// same index; slot word 0xffffffff: none), then closest-hit walk, shading,
-// connection and shadow walk bounce after bounce.  A path executes exactly
-// the operations of the wavefront kernels in the same order (a connection is
-// applied before the next bounce is shaded), so results are identical.
+// of the wave left by the last bounce launch run (t, the switch bounce or K)
+// through all its remaining bounces on one lane, each at its own depth: the
+// connection attached to it by that launch (queue (t - 1) & 1, same index;
+// slot word 0xffffffff: none), then closest-hit walk, shading, connection and
+// shadow walk bounce after bounce; then the walks that launch carried,
+// resumed where they stopped.  A path executes exactly the operations of the
+// wavefront kernels in the same order (a connection is applied before the
+// next bounce is shaded), so results are identical.
 enum : uint32_t { kIdle = 0, kPathExt = 1, kPathShadow = 2 };
 
 // walk steps of the tail kernel between two refill checks: a lane whose walk
@@ -745,20 +818,25 @@ enum : uint32_t { kIdle = 0, kPathExt = 1, kPathShadow = 2 };
 __host__ __device__ constexpr int tail_steps() { return 64; }
 
 template <bool kCount, bool kWide>
-__global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, RenderBuffers b, int in, int shIn,
-                                                   uint32_t depth0, uint32_t kRefill) {
-  const uint32_t n = in >= 0 ? b.ctr->wave[in] : 0u;
-  const uint32_t nCarry = b.carry ? min(b.ctr->carryN, b.carryCap) : 0u;
+__global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, RenderBuffers b, uint32_t K,
+                                                   uint32_t kRefill) {
+  // t: the launch the bounce launches stopped before (the device switch or K)
+  const uint32_t t = min(b.ctr->tailAt, K);
+  const int in = (int)(t & 1u);
+  const int shIn = t > 0 ? (int)((t - 1) & 1u) : -1;
+  const uint32_t n = b.ctr->wave[in];
+  const uint32_t nCarry = t > 0 ? carried_of(b, t - 1) : 0u;
+  const float4* carried = b.carry[(t + 1) & 1u];  // launch t - 1's
   const uint32_t total = n + nCarry;
   const uint32_t cacheSize = b.lctr->cacheSize[a.cacheSel];
   const float4* __restrict__ cache = b.cache[a.cacheSel];
   const float4* __restrict__ sh = b.sh[shIn >= 0 ? shIn : 0];
-  const Wave wv = b.wave[in >= 0 ? in : 0];
+  const Wave wv = b.wave[in];
   const uint32_t lane = threadIdx.x & 31;
   typename WalkOf<kWide>::type w;
   typename WalkOf<kWide>::Entry stack[WalkOf<kWide>::kDepth];
   PathIO io;
-  uint32_t mode = kIdle, depth = 0;
+  uint32_t mode = kIdle;
   bool drained = false, resumed = false;
   uint32_t extRays = 0, shRays = 0, nnE = 0, ntE = 0, nnS = 0, ntS = 0;
   for (;;) {
@@ -773,40 +851,19 @@ __global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, Ren
       if (mode == kIdle) {
         const uint32_t j = base + __popc(idle & lanemask_lt());
         if (j >= n && j < total) {  // a carried walk: resume it where it stopped
-          const float4* r = b.carry + (size_t)(j - n) * kCarryF4;
+          const float4* r = carried + (size_t)(j - n) * kCarryF4;
           io.o = r[0];
           io.d = r[1];
           io.t = r[2];
           io.s = r[3];
-          depth = __float_as_uint(r[3].w);
           mode = kPathExt;
           resumed = true;
-          w.init(ld3(io.o), ld3(io.d), gb::kInf, gb::kBias, stack);
-          if constexpr (!kWide) {
-            const float4 q = r[4], z = r[5];
-            w.minT = q.x;
-            w.best = __float_as_uint(q.y);
-            w.bu = q.z;
-            w.bv = q.w;
-            w.bw = z.x;
-            w.steps = __float_as_uint(z.y);
-            w.tos = __float_as_uint(z.z);
-            w.sp = __float_as_int(z.w);
-#pragma unroll
-            for (int k = 0; k < 8; k++) {
-              const float4 e = r[6 + k];
-              stack[4 * k] = __float_as_uint(e.x);
-              stack[4 * k + 1] = __float_as_uint(e.y);
-              stack[4 * k + 2] = __float_as_uint(e.z);
-              stack[4 * k + 3] = __float_as_uint(e.w);
-            }
-          }
+          if constexpr (!kWide) resume_walk(r, w, stack);
         } else if (j < n) {
           io.o = wv.o[j];
           io.d = wv.d[j];
           io.t = wv.thr[j];
           io.s = wv.smp[j];
-          depth = depth0;
           const float4 A = (shIn >= 0) ? sh[3 * (size_t)j] : make_float4(0.f, 0.f, 0.f, __uint_as_float(0xffffffffu));
           if (__float_as_uint(A.w) != 0xffffffffu) {
             io.shA = A;
@@ -837,7 +894,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, Ren
         const float4 r = b.res[slot];
         b.res[slot] = make_float4(r.x + io.shC.x, r.y + io.shC.y, r.z + io.shC.z,
                                   __uint_as_float(__float_as_uint(r.w) + 4u));
-        if (a.bilat && depth <= 1) direct_connect(b.dsm, slot, io.shC);
+        if (a.bilat && __float_as_uint(io.shC.w) == 0u) direct_connect(b.dsm, slot, io.shC);  // made at bounce 0
       }
       mode = kPathExt;  // the path's next extension ray
       w.init(ld3(io.o), ld3(io.d), gb::kInf, gb::kBias, stack);
@@ -849,11 +906,10 @@ __global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, Ren
     resumed = false;
     const float4 h4 = w.hit() ? make_float4(w.minT, __uint_as_float(w.best), w.bu, w.bv)
                               : make_float4(-1.f, 0.f, 0.f, 0.f);
-    shade_path(S, a, b, cache, cacheSize, depth, h4, io);
+    shade_path(S, a, b, cache, cacheSize, __float_as_uint(io.s.w), h4, io);
     if (!io.cont) {
       mode = kIdle;
     } else {
-      depth++;
       if (io.conn) {
         mode = kPathShadow;
         w.init(ld3(io.shA), ld3(io.shB), io.shB.w, gb::kBias, stack);
@@ -1101,45 +1157,43 @@ uint32_t persistent_grid(uint32_t full, uint32_t ctasPerSm) {
 }
 
 template <bool kCount, bool kWide>
-void walk_variant(const DevScene& S, const RenderBuffers& b, int in, int shIn, int shReset, uint32_t sd,
-                  uint32_t refill, uint32_t ctas, uint32_t depth, uint32_t carrySteps, cudaStream_t st) {
+void walk_variant(const DevScene& S, const RenderBuffers& b, int in, int shIn, int shReset, uint32_t bilat,
+                  uint32_t refill, uint32_t ctas, uint32_t launch, uint32_t carrySteps, cudaStream_t st) {
   const uint32_t g = persistent_grid(walk_grid<kCount, kWide>(), ctas);
-  k_walk<kCount, kWide><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, sd, refill, depth, carrySteps);
+  k_walk<kCount, kWide><<<g, kBlock, 0, st>>>(S, b, in, shIn, shReset, bilat, refill, launch, carrySteps);
 }
 
 template <bool kCount, bool kWide>
-void tail_variant(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn, uint32_t depth0,
-                  cudaStream_t st) {
+void tail_variant(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, uint32_t K, cudaStream_t st) {
   const uint32_t g = persistent_grid(tail_grid<kCount, kWide>(), a.walkCtas);
-  k_tail<kCount, kWide><<<g, kBlock, 0, st>>>(S, a, b, in, shIn, depth0, walk_refill_for(a.refill, kWide));
+  k_tail<kCount, kWide><<<g, kBlock, 0, st>>>(S, a, b, K, walk_refill_for(a.refill, kWide));
 }
 
 cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
-                        int shReset, bool shDirect, uint32_t depth, cudaStream_t st) {
-  const uint32_t sd = (a.bilat && shDirect) ? 1u : 0u;
+                        int shReset, uint32_t launch, cudaStream_t st) {
+  const uint32_t sd = a.bilat ? 1u : 0u;
   const bool wide = S.traversal == 1 && S.wide;
   const uint32_t rf = walk_refill_for(a.refill, wide);
-  const uint32_t cs = b.carry ? a.carrySteps : 0u;
+  const uint32_t cs = b.carry[0] ? a.carrySteps : 0u;
   if (a.counting) {
-    if (wide) walk_variant<true, true>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, depth, 0u, st);
-    else walk_variant<true, false>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, depth, cs, st);
+    if (wide) walk_variant<true, true>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, launch, 0u, st);
+    else walk_variant<true, false>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, launch, cs, st);
   } else {
-    if (wide) walk_variant<false, true>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, depth, 0u, st);
-    else walk_variant<false, false>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, depth, cs, st);
+    if (wide) walk_variant<false, true>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, launch, 0u, st);
+    else walk_variant<false, false>(S, b, in, shIn, shReset, sd, rf, a.walkCtas, launch, cs, st);
   }
   note_launches(1);
   return cudaGetLastError();
 }
 
-cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
-                        uint32_t depth0, cudaStream_t st) {
+cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, uint32_t K, cudaStream_t st) {
   const bool wide = S.traversal == 1 && S.wide;
   if (a.counting) {
-    if (wide) tail_variant<true, true>(S, a, b, in, shIn, depth0, st);
-    else tail_variant<true, false>(S, a, b, in, shIn, depth0, st);
+    if (wide) tail_variant<true, true>(S, a, b, K, st);
+    else tail_variant<true, false>(S, a, b, K, st);
   } else {
-    if (wide) tail_variant<false, true>(S, a, b, in, shIn, depth0, st);
-    else tail_variant<false, false>(S, a, b, in, shIn, depth0, st);
+    if (wide) tail_variant<false, true>(S, a, b, K, st);
+    else tail_variant<false, false>(S, a, b, K, st);
   }
   note_launches(1);
   return cudaGetLastError();
@@ -1181,10 +1235,10 @@ uint32_t walk_refill_for(uint32_t requested, bool wide) {
   return wide ? 20u : 8u;
 }
 
-cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t depth,
+cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t launch,
                          bool attach, cudaStream_t st) {
   const uint32_t g = shade_grid();
-  k_shade<<<g, kBlock, 0, st>>>(S, a, b, in, depth, attach ? 1u : 0u);
+  k_shade<<<g, kBlock, 0, st>>>(S, a, b, in, launch, attach ? 1u : 0u);
   note_launches(1);
   return cudaGetLastError();
 }

@@ -56,16 +56,19 @@ struct DevCounters {
   unsigned long long rays, nodes, tris;  // cumulative work counters (closest-hit walks)
   unsigned long long shadowRays, nodesS, trisS;  // any-hit (shadow) walks
   double errSum;          // adaptive: sum of per-pixel errors
-  uint32_t carryN;        // extension walks handed from the bounce launches to the tail kernel this frame
+  uint32_t carryN[3];     // extension walks carried out of bounce launch L, in counter L % 3
   uint32_t fetchTail;     // next item handed to a lane by the tail kernel
+  uint32_t tailAt;        // bounce from which the tail kernel carries the frame's paths, when a shading
+                          // launch found fewer live paths than FrameArgs::tailBelow (~0u: no switch)
 };
 
 // Path state of one wavefront (structure of arrays, float4-packed).
 struct Wave {
   float4* o;    // origin.xyz, slot (uint bits)
-  float4* d;    // direction.xyz, depth | type << 8
-  float4* thr;  // throughput (pathOutMulTerm).xyz
-  float4* smp;  // carried emission (pathSample).xyz
+  float4* d;    // direction.xyz, pixel id (uint bits)
+  float4* thr;  // throughput (pathOutMulTerm).xyz, path potential (filter-only mode)
+  float4* smp;  // carried emission (pathSample).xyz, the path's depth (uint bits): waves mix
+                // depths once carried walks rejoin a launch one bounce behind
 };
 
 struct FrameArgs {
@@ -92,9 +95,14 @@ struct FrameArgs {
   // height the window's
   uint32_t winX0, winY0, fullW;
   // walk steps a warp keeps stepping its extension walks after the launch's
-  // ray queue ran dry before it carries the unfinished ones to the tail kernel
-  // (0: never; the reference-order walk only)
+  // ray queue ran dry before it carries the unfinished ones to the next
+  // launch (0: never; the reference-order walk only)
   uint32_t carrySteps;
+  // live paths, as a fraction of the band's camera paths, below which the
+  // shading launch of a bounce hands the remaining bounces to the tail kernel
+  // (decided on the device from the bounce's path count; 0: the fixed switch
+  // bounce alone)
+  float tailBelow;
 };
 
 struct RenderBuffers {
@@ -123,10 +131,11 @@ struct RenderBuffers {
   uint32_t base;
   uint32_t count;
   // extension walks still running when a bounce launch's other work is done
-  // are handed over (carried) to the frame's tail kernel instead of being
-  // waited for: kCarryF4 float4 per walk (the path, its depth, the walk's state
-  // and stack), up to carryCap walks per frame and band
-  float4* carry;
+  // are handed over (carried) to the next bounce launch, or the tail kernel,
+  // instead of being waited for: kCarryF4 float4 per walk (the path with its
+  // depth, the walk's state and stack), up to carryCap walks per launch and
+  // band, launch L's in buffer L & 1
+  float4* carry[2];
   uint32_t carryCap;
 };
 constexpr uint32_t kMaxBands = 8;
@@ -135,22 +144,20 @@ constexpr uint32_t kCarryF4 = 14;
 // wavefront kernels (kernels_wave.cu)
 cudaError_t launch_light_pass(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, cudaStream_t st);
 cudaError_t launch_camera(const FrameArgs& a, const RenderBuffers& b, cudaStream_t st);
-// one persistent walk over the extension rays of wave `in` (in < 0: none)
-// followed by the shadow rays of connection queue `shIn` (shIn < 0: none);
-// resets the counters of wave in^1 and of connection queue `shReset`
-// (shDirect: the connection queue holds bounce-0 connections, which update
-// the direct-light sample of the filter-only mode)
-// (depth: the bounce of wave `in`'s extension rays, recorded with a carried walk)
+// bounce launch L's persistent walk: the walks launch L - 1 carried (when it
+// has a wave), the extension rays of wave `in` (in < 0: none), then the
+// shadow rays of connection queue `shIn` (shIn < 0: none); resets the
+// counters of wave in^1 and of connection queue `shReset`
 cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
-                        int shReset, bool shDirect, uint32_t depth, cudaStream_t st);
+                        int shReset, uint32_t launch, cudaStream_t st);
 // attach: store each continuing path's connection at the path's index (for the tail kernel)
-cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t depth,
+cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t launch,
                          bool attach, cudaStream_t st);
-// remaining bounces of every path of wave `in` (at bounce depth0; in < 0: no
-// wave), starting with the connection attached to it in queue shIn, then of
-// every walk the bounce launches carried; one lane per path
-cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, int shIn,
-                        uint32_t depth0, cudaStream_t st);
+// remaining bounces of every path alive at bounce t = min(switch bounce the
+// shading launches recorded, K) when t is below the depth cap (wave t & 1,
+// starting with the connection attached to each path in queue (t - 1) & 1),
+// then of every walk the bounce launches carried; one lane per path
+cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, uint32_t K, cudaStream_t st);
 // first bounce handled by the tail kernel: `requested` when >= 0 (>= D: none),
 // else GBPT_TAIL_FROM when set, else D/2 - 1 (wide order: D/2) for D > 6 and
 // none for D <= 6

@@ -20,11 +20,13 @@
 // with GBPT_ERR_OOM only when no other request is running.
 //
 // Autotuning: the walks' refill threshold, the bounce from which the tail
-// kernel carries the remaining paths, the bands a frame is split into and the
-// persistent grids' CTAs per SM change scheduling and launch shape only --
-// every path executes the same operations in the same order -- so images are
-// identical whichever values run.  Requests that leave them at their defaults
-// (walk_refill 0, tail_from -1, bands 0, walk_ctas 0) are assigned a candidate
+// kernel carries the remaining paths (fixed, or decided on the device below a
+// live-path fraction), the bands a frame is split into and the persistent
+// grids' CTAs per SM change scheduling and launch shape only -- every path
+// executes the same operations in the same order -- so images are identical
+// whichever values run.  Requests that leave them at their defaults
+// (walk_refill 0, tail_from -1, bands 0, walk_ctas 0, tail_below the
+// library's default) are assigned a candidate
 // per class (mode,
 // depth cap, image size rounded to a power of two); each candidate is timed
 // on whole requests (device time per camera path) until it has kTrials
@@ -68,8 +70,9 @@ struct Knobs {
   int32_t tail;    // -1: the library's rule
   uint32_t bands;  // wavefronts per frame
   uint32_t ctas;   // CTAs per SM of the persistent walk and tail grids (0: as many as fit)
+  float below;     // live-path fraction below which the device switches to the tail kernel
   bool operator==(const Knobs& o) const {
-    return refill == o.refill && tail == o.tail && bands == o.bands && ctas == o.ctas;
+    return refill == o.refill && tail == o.tail && bands == o.bands && ctas == o.ctas && below == o.below;
   }
 };
 
@@ -79,15 +82,18 @@ struct Knobs {
 // large workloads (small images favour earlier refills and earlier tails,
 // whose per-bounce launches wait on their slowest ray), then launch shapes:
 // persistent grids of 2 or 3 CTAs per SM, which leave SMs to the requests
-// running beside, and two bands for images of 512K pixels and more.
-std::vector<Knobs> candidates(uint32_t depth, uint32_t sizeLog2) {
-  std::vector<Knobs> c = {{8, -1, 1, 0}, {4, -1, 1, 0}, {16, -1, 1, 0}};
-  if (depth > 3) c.push_back({8, (int32_t)depth - 3, 1, 0});
-  if (depth > 5) c.push_back({8, (int32_t)depth - 5, 1, 0});
-  c.push_back({8, (int32_t)depth, 1, 0});  // no tail kernel
-  c.push_back({8, -1, 1, 2});
-  c.push_back({8, -1, 1, 3});
-  if (sizeLog2 >= 19) c.push_back({8, -1, 2, 0});
+// running beside, two bands for images of 512K pixels and more, and the tail
+// switch decided on the device at two live-path fractions.
+std::vector<Knobs> candidates(uint32_t depth, uint32_t sizeLog2, float below) {
+  std::vector<Knobs> c = {{8, -1, 1, 0, below}, {4, -1, 1, 0, below}, {16, -1, 1, 0, below}};
+  if (depth > 3) c.push_back({8, (int32_t)depth - 3, 1, 0, below});
+  if (depth > 5) c.push_back({8, (int32_t)depth - 5, 1, 0, below});
+  c.push_back({8, (int32_t)depth, 1, 0, 0.f});  // no tail kernel but the carried walks'
+  c.push_back({8, -1, 1, 2, below});
+  c.push_back({8, -1, 1, 3, below});
+  if (sizeLog2 >= 19) c.push_back({8, -1, 2, 0, below});
+  for (float f : {0.25f, 0.5f})
+    if (f != below) c.push_back({8, (int32_t)depth, 1, 0, f});
   return c;
 }
 
@@ -117,7 +123,7 @@ struct Request {
   gbpt_request q{};
   gbpt_params p{};
   bool tuned = false;  // knobs come from the autotuner
-  Knobs knobs{0, -1, 0, 0};
+  Knobs knobs{0, -1, 0, 0, 0.f};
   Clock::time_point tSubmit, tStart, tEnd;
   gbpt_status status = GBPT_OK;
   std::string err;
@@ -169,7 +175,9 @@ struct gbpt_server {
   Knobs assign(const ClassKey& k) {
     Tuning& t = tuning[k];
     if (t.cand.empty()) {
-      t.cand = candidates(k.depth, k.size);
+      gbpt_params dflt;
+      gbpt_params_default(&dflt);
+      t.cand = candidates(k.depth, k.size, dflt.tail_below);
       t.msPerPath.assign(t.cand.size(), 0.0);
       t.trials.assign(t.cand.size(), 0);
     }
@@ -254,6 +262,7 @@ static gbpt_status run_request(gbpt_server* srv, Pool& pool, Request& q, std::st
     p.tail_from = q.knobs.tail;
     p.bands = q.knobs.bands;
     p.walk_ctas = q.knobs.ctas;
+    p.tail_below = q.knobs.below;
   }
   gbpt_renderer* r = nullptr;
   {
@@ -402,8 +411,11 @@ gbpt_status gbpt_server_submit(gbpt_server* s, const gbpt_request* req, uint64_t
   } else {
     gbpt_params_default(&q->p);
   }
-  q->tuned = q->p.walk_refill == 0 && q->p.tail_from == -1 && q->p.bands == 0 && q->p.walk_ctas == 0;
-  q->knobs = Knobs{q->p.walk_refill, q->p.tail_from, q->p.bands, q->p.walk_ctas};
+  gbpt_params dflt;
+  gbpt_params_default(&dflt);
+  q->tuned = q->p.walk_refill == 0 && q->p.tail_from == -1 && q->p.bands == 0 && q->p.walk_ctas == 0 &&
+             q->p.tail_below == dflt.tail_below;
+  q->knobs = Knobs{q->p.walk_refill, q->p.tail_from, q->p.bands, q->p.walk_ctas, q->p.tail_below};
   q->tSubmit = Clock::now();
   {
     std::lock_guard<std::mutex> lock(s->mu);
@@ -460,11 +472,12 @@ gbpt_status gbpt_server_tuned_params(gbpt_server* s, int32_t mode, uint32_t dept
   auto it = s->tuning.find(ClassKey{mode, depth, probe.size()});
   *samples = 0;
   if (it == s->tuning.end()) {
-    const Knobs k = candidates(depth, probe.size())[0];
+    const Knobs k = candidates(depth, probe.size(), knobs->tail_below)[0];
     knobs->walk_refill = k.refill;
     knobs->tail_from = k.tail;
     knobs->bands = k.bands;
     knobs->walk_ctas = k.ctas;
+    knobs->tail_below = k.below;
     return GBPT_OK;
   }
   const Tuning& t = it->second;
@@ -473,6 +486,7 @@ gbpt_status gbpt_server_tuned_params(gbpt_server* s, int32_t mode, uint32_t dept
   knobs->tail_from = k.tail;
   knobs->bands = k.bands;
   knobs->walk_ctas = k.ctas;
+  knobs->tail_below = k.below;
   for (uint32_t n : t.trials) *samples += n;
   return GBPT_OK;
 }

@@ -70,6 +70,7 @@ PARAMS = np.dtype(
         ("bands", "<u4"),
         ("walk_ctas", "<u4"),
         ("carry_steps", "<u4"),
+        ("tail_below", "<f4"),
     ]
 )
 
@@ -123,7 +124,8 @@ def default_params(**over):
     p["tail_from"] = -1
     p["bands"] = 0
     p["walk_ctas"] = 0
-    p["carry_steps"] = 96
+    p["carry_steps"] = 64
+    p["tail_below"] = 0.0
     for k, v in over.items():
         p[k] = v
     return p

@@ -79,13 +79,13 @@ class Server:
 
     def tuned_knobs(self, mode, depth, width, height):
         """Every knob the autotuner holds for a request class: dict(walk_refill,
-        tail_from, bands, walk_ctas, samples)."""
+        tail_from, bands, walk_ctas, tail_below, samples)."""
         p = layouts.default_params()
         n = ctypes.c_uint32()
         check(load().gbpt_server_tuned_params(self._h, int(mode), int(depth), int(width), int(height),
                                               p.ctypes.data, ctypes.addressof(n)))
         return dict(walk_refill=int(p["walk_refill"]), tail_from=int(p["tail_from"]), bands=int(p["bands"]),
-                    walk_ctas=int(p["walk_ctas"]), samples=n.value)
+                    walk_ctas=int(p["walk_ctas"]), tail_below=float(p["tail_below"]), samples=n.value)
 
     def close(self):
         """Finishes queued and running requests, then frees the renderers."""

@@ -112,7 +112,12 @@ typedef struct gbpt_params {
                                fewer leave SMs to other requests that share the GPU */
   uint32_t carry_steps;     /* walk steps a bounce launch keeps stepping its last extension walks after
                                its ray queue ran dry before handing the unfinished ones, mid-walk, to the
-                               frame's tail kernel (0: never; default 96; the reference-order walk only) */
+                               next bounce launch (or the tail kernel), where they finish and are shaded one
+                               bounce behind (0: never; default 64; <= 2^20; the reference-order walk only) */
+  float tail_below;         /* live paths, as a fraction of the frame's (band's) camera paths, below which a
+                               bounce's shading launch hands the remaining bounces to the tail kernel,
+                               decided on the device from the bounce's path count ([0, 1]; 0: tail_from
+                               alone); the switch comes at tail_from at the latest */
 } gbpt_params;
 
 /* Renderer modes: the BDPT entries of the X-macro registry

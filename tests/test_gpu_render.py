@@ -208,6 +208,11 @@ def test_errors_are_reported(gbdev):
         r.render(s, cam)
     with pytest.raises(gb.GbptError):
         gb.RTRenderer(16, 16, params=gb.default_params(light_paths=5000))
+    for below in (-0.5, 1.5, float("nan")):
+        with pytest.raises(gb.GbptError, match="tail_below"):
+            gb.RTRenderer(16, 16, params=gb.default_params(tail_below=below))
+    with pytest.raises(gb.GbptError, match="carry_steps"):
+        gb.RTRenderer(16, 16, params=gb.default_params(carry_steps=(1 << 20) + 1))
     with pytest.raises(gb.GbptError):
         r.attr_set("No Such Attribute", 1.0)
 
@@ -383,6 +388,38 @@ def test_bands_change_no_pixel(gbdev, orc, mode):
                                                          render_iterations=3))
     ref.render(orc.Scene(v, t, m), cam, 4)
     assert_bits_equal(base[0], ref.get(0), "image against the oracle")
+
+
+@pytest.mark.parametrize("mode,depth", [(0, 10), (1, 6), (4, 8)])
+def test_carry_and_tail_switch_change_no_pixel(gbdev, mode, depth):
+    """Walks carried mid-walk from the bounce launches to the tail kernel
+    (carry_steps; at 1 step the carry buffer fills and the other walks finish
+    in their launch) and the switch to the tail kernel decided on the device
+    (tail_below) move work between kernels only: image, sample counts and ray
+    counts equal those of per-bounce launches throughout, in both traversal
+    orders (the wide walk carries nothing)."""
+    (v, t, m), cam = scene_arrays("interior")
+    W, H = 96, 72
+    runs = {}
+    for order in ("reference", "wide"):
+        s = gbdev.RTScene(v, t, m).build_bvh()
+        s.set_traversal(order)
+        for cs, below, tail in ((0, 0.0, depth), (96, 0.0, depth), (1, 0.0, depth), (0, 0.5, depth),
+                                (96, 0.3, -1), (1, 0.95, -1), (4, 1.0, 2)):
+            p = gbdev.default_params(eye_depth_max=depth, light_depth_max=depth, pt_depth_max=depth, carry_steps=cs,
+                                     tail_below=below, tail_from=tail, warmup_frames=2)
+            r = gbdev.RTRenderer(W, H, mode, p)
+            rays = 0
+            for _ in range(4):
+                r.render(s, cam, stats=True)
+                rays += r.last_stats["rays"]
+            runs[order, cs, below, tail] = (r.read_buffer(0), r.read_buffer(6), rays)
+            r.close()
+    base = runs["reference", 0, 0.0, depth]
+    for key, (img, sn, rays) in runs.items():
+        assert_bits_equal(img, base[0], f"image {key}")
+        assert_bits_equal(sn, base[1], f"sampleN {key}")
+        assert rays == base[2], (key, rays, base[2])
 
 
 @pytest.mark.parametrize("mode", [0, 3, 4])

@@ -405,7 +405,11 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, uint32_t v
 // are independent, so running them in one launch removes one kernel tail per
 // bounce.  A lane takes a new ray as soon as its ray is finished (refill when
 // at least kRefill lanes of the warp are idle), so warps stay full while rays
-// last; extension rays are handed out first (they are the longer walks).
+// last.  Shadow rays are handed out first: they cannot be carried to the next
+// launch (a path's connection contributions are summed in bounce order), so
+// the long ones must start early; then the walks the previous launch carried,
+// then the extension rays (hall 1280x720: 181.4 -> 187.9 Mpaths/s against
+// extension rays first; interior 169.0 -> 168.2).
 // Every ray still visits nodes exactly in TracePrimitive's order, so per-ray
 // results do not depend on this scheduling.  The any-hit walk stops at the
 // first hit closer than maxDist: that is exactly when the reference's
@@ -543,9 +547,9 @@ __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, Rend
         const uint32_t k = base + __popc(idle & lanemask_lt());
         if (k < n) {
           has = true;
-          any = k >= nCE;
-          res = k < nC;
-          item = any ? k - nCE : (res ? k : k - nC);
+          any = k < nS;
+          res = !any && k < nS + nC;
+          item = any ? k : (res ? k - nS : k - nS - nC);
           if (any) {
             const float4 A = sh[3 * (size_t)item], B = sh[3 * (size_t)item + 1];
             w.init(ld3(A), ld3(B), B.w, gb::kBias, stack);

@@ -353,6 +353,8 @@ struct gbpt_renderer {
     dfree(rb.ctr);
     dfree(rb.carry[0]);
     dfree(rb.carry[1]);
+    dfree(rb.conn);
+    rb.connDepth = 0;
     dfree(ab.err);
     dfree(ab.cnt);
     dfree(ab.off);
@@ -455,12 +457,12 @@ RenderBuffers band_buffers(const RenderBuffers& rb, uint32_t b, uint32_t k, size
     x.wave[w].thr += p0;
     x.wave[w].smp += p0;
   }
-  x.hit += p0;
+  const size_t c0 = (size_t)rb.carryCap * b / k, c1 = (size_t)rb.carryCap * (b + 1) / k;
+  x.hit += p0 + c0;  // the band's paths and the walks it resumes: count + its carry records
   x.sh[0] += 3 * p0;
   x.sh[1] += 3 * p0;
   x.ctr = rb.ctr + b;
   x.lctr = rb.ctr;
-  const size_t c0 = (size_t)rb.carryCap * b / k, c1 = (size_t)rb.carryCap * (b + 1) / k;
   x.carry[0] = rb.carry[0] + c0 * kCarryF4;
   x.carry[1] = rb.carry[1] + c0 * kCarryF4;
   x.carryCap = (uint32_t)(c1 - c0);
@@ -473,7 +475,8 @@ uint64_t gbpt::renderer_bytes(uint32_t W, uint32_t H, const gbpt_params& p) {
   const size_t np = (size_t)W * H;
   const uint32_t cacheCap = std::max(1u, p.light_paths * (1 + p.light_depth_max));
   return np * (128 + 16 + 96 + 16 + 48 + 16 + 8) + np * (12 * 10 + 4 * 2 + 4 * 5) + (size_t)cacheCap * 192 +
-         2 * std::max<size_t>(np / 8, 256) * kCarryF4 * 16;
+         std::max<size_t>(np / 8, 256) * (2 * kCarryF4 + 1) * 16 +
+         np * 16 * (std::max(std::max(p.eye_depth_max, p.pt_depth_max), 2u) - 1);
 }
 
 namespace {
@@ -495,7 +498,10 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
     float4* b = r->waveMem + (size_t)k * 4 * cap;
     r->rb.wave[k] = Wave{b, b + cap, b + 2 * cap, b + 3 * cap};
   }
-  CK(dalloc(&r->rb.hit, cap));
+  // hit words: one per live path of the wave, plus one per walk a launch
+  // resumes (carried connection walks are not paths: they take words past the paths')
+  r->rb.carryCap = (uint32_t)std::max<size_t>(cap / 8, 256);
+  CK(dalloc(&r->rb.hit, cap + r->rb.carryCap));
   CK(dalloc(&r->rb.sh[0], cap * 3));
   CK(dalloc(&r->rb.sh[1], cap * 3));
   CK(dalloc(&r->rb.res, cap));
@@ -505,7 +511,6 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
   CK(dalloc(&r->rb.slotSmp, cap));
   CK(dalloc(&r->rb.cache[0], (size_t)cacheCap * 6));
   CK(dalloc(&r->rb.cache[1], (size_t)cacheCap * 6));
-  r->rb.carryCap = (uint32_t)std::max<size_t>(cap / 8, 256);
   CK(dalloc(&r->rb.carry[0], (size_t)r->rb.carryCap * kCarryF4));
   CK(dalloc(&r->rb.carry[1], (size_t)r->rb.carryCap * kCarryF4));
   CK(dalloc(&r->rb.ctr, kMaxBands));
@@ -793,8 +798,8 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
     // last launch walks the final connections instead of the tail kernel.
     const uint32_t D = a.eyeDepth;
     const bool wideT = S.traversal == 1 && S.wide;
-    const uint32_t K = std::min(tail_from(D, wideT, r->p.tail_from), D);
     const bool carrying = a.carrySteps && !wideT;
+    const uint32_t K = std::min(tail_from(D, wideT, r->p.tail_from), D);
     const bool tailRun = K < D || carrying || a.tailBelow > 0.f;
     auto bounces = [&](const RenderBuffers& rbx, cudaStream_t sx, bool mk) -> gbpt_status {
       int in = 0;
@@ -812,6 +817,7 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
         // terminate without connecting; kept so the sequence needs no special case)
         CK(launch_walk(S, a, rbx, -1, (int)((D - 1) & 1u), (int)(D & 1u), D, sx));
       }
+      CK(launch_fold(rbx, sx));
       return GBPT_OK;
     };
     const size_t np = (size_t)r->W * r->H;
@@ -950,12 +956,29 @@ const float* output_view(const gbpt_renderer* r) {
   return (r->debugMode == 4.f && r->mode != GBPT_MODE_BDPT_SC) ? r->ab.filtered : r->result;
 }
 
+// The per-bounce connection entries for the renderer's depth caps, grown when
+// a cap grows (D - 1 bounces make connections: paths end at the cap).
+gbpt_status ensure_conn(gbpt_renderer* r) {
+  const uint32_t need = std::max(std::max(r->p.eye_depth_max, r->p.pt_depth_max), 2u) - 1;
+  if (r->rb.conn && r->rb.connDepth >= need) return GBPT_OK;
+  if (r->rb.conn) {
+    CK(cudaStreamSynchronize(r->st));
+    dfree(r->rb.conn);
+  }
+  r->rb.connDepth = 0;
+  CK(dalloc(&r->rb.conn, (size_t)r->rb.cap * need));
+  r->rb.connDepth = need;
+  return GBPT_OK;
+}
+
 gbpt_status render_impl(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, uint32_t frames, float* out,
                         int32_t outDev, gbpt_stats* stats) {
   if (!r || !s || !cam) return fail(GBPT_ERR_INVALID_ARG, "NULL renderer, scene or camera");
   gbpt_status stt = ensure_uploaded(s);
   if (stt != GBPT_OK) return stt;
   stt = ensure_alloc(r);
+  if (stt != GBPT_OK) return stt;
+  stt = ensure_conn(r);
   if (stt != GBPT_OK) return stt;
   DevCounters before{};
   const bool timing = stats != nullptr;

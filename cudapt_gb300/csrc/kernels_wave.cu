@@ -426,32 +426,37 @@ __host__ __device__ constexpr int walk_steps() {
   return kWide ? 2 : 6;
 }
 
-// One carried walk to carry buffer `dst` (out of line: it runs for a few
-// walks per launch, and keeping it out of the walk loop keeps that loop's
-// registers): the path (po..ps, its depth in ps.w), the walk's state and its
-// node stack; false when the buffer is full.
-__device__ __noinline__ bool save_carry(float4* dst, uint32_t* cnt, uint32_t cap, const float4* po,
-                                        const float4* pd, const float4* pt, const float4* ps, float minT,
+// Word 3.w of a carry record: the path's depth for an extension walk, this
+// tag for a connection (shadow) walk, whose record holds the connection
+// {origin, slot} {direction, maxDist} {contribution, bounce} instead of the path.
+constexpr uint32_t kShadowRec = 0xFFFFFFFFu;
+
+// One carried walk to carry record r (out of line: it runs for a few walks
+// per launch, and keeping it out of the walk loop keeps that loop's
+// registers): three float4 of the walk's ray at src, src + stride, src +
+// 2 * stride (the path of a wave, or a connection record), the fourth at src
+// + 3 * stride (the path's carried emission and depth) or the connection tag,
+// then the walk's state and its node stack.
+__device__ __noinline__ void save_carry(float4* r, const float4* src, size_t stride, bool shadow, float minT,
                                         uint32_t best, float bu, float bv, float bw, uint32_t steps, uint32_t tos,
                                         int sp, const uint32_t* stack) {
-  const uint32_t c = atomicAdd(cnt, 1u);
-  if (c >= cap) return false;
-  float4* r = dst + (size_t)c * kCarryF4;
-  r[0] = *po;
-  r[1] = *pd;
-  r[2] = *pt;
-  r[3] = *ps;
+  r[0] = src[0];
+  r[1] = src[stride];
+  r[2] = src[2 * stride];
+  r[3] = shadow ? make_float4(0.f, 0.f, 0.f, __uint_as_float(kShadowRec)) : src[3 * stride];
   r[4] = make_float4(minT, __uint_as_float(best), bu, bv);
   r[5] = make_float4(bw, __uint_as_float(steps), __uint_as_float(tos), __int_as_float(sp));
   for (int k = 0; k < 8; k++)
     r[6 + k] = make_float4(__uint_as_float(stack[4 * k]), __uint_as_float(stack[4 * k + 1]),
                            __uint_as_float(stack[4 * k + 2]), __uint_as_float(stack[4 * k + 3]));
-  return true;
 }
 
-// The walk of carry record r, resumed at the step where it stopped.
-__device__ __forceinline__ void resume_walk(const float4* r, Walk& w, uint32_t* stack) {
-  w.init(ld3(r[0]), ld3(r[1]), gb::kInf, gb::kBias, stack);
+// The walk of carry record r, resumed at the step where it stopped; true for
+// a connection walk (any hit up to its maxDist).
+__device__ __forceinline__ bool resume_walk(const float4* r, Walk& w, uint32_t* stack) {
+  const float4 r1 = r[1];
+  const bool shadow = __float_as_uint(r[3].w) == kShadowRec;
+  w.init(ld3(r[0]), ld3(r1), shadow ? r1.w : gb::kInf, gb::kBias, stack);
   const float4 q = r[4], z = r[5];
   w.minT = q.x;
   w.best = __float_as_uint(q.y);
@@ -469,6 +474,16 @@ __device__ __forceinline__ void resume_walk(const float4* r, Walk& w, uint32_t* 
     stack[4 * k + 2] = __float_as_uint(e.z);
     stack[4 * k + 3] = __float_as_uint(e.w);
   }
+  return shadow;
+}
+
+// An unoccluded connection: its contribution into the slot's entry for the
+// bounce that made it (summed with the path's other connections, in bounce
+// order, by k_fold once every walk of the frame is done).
+__device__ __forceinline__ void connection_reached(const RenderBuffers& b, uint32_t bilat, float4 A, float4 C) {
+  const uint32_t slot = __float_as_uint(A.w), bounce = __float_as_uint(C.w);
+  b.conn[(size_t)bounce * b.cap + slot] = make_float4(C.x, C.y, C.z, 1.f);
+  if (bilat && bounce == 0u) direct_connect(b.dsm, slot, C);
 }
 
 // walks carried out of bounce launch L (buffer L & 1, counter L % 3; the
@@ -478,17 +493,20 @@ __device__ __forceinline__ uint32_t carried_of(const RenderBuffers& b, uint32_t 
 }
 
 // Carrying (reference order only): once the launch's ray queue is empty, a
-// warp keeps stepping its walks for carrySteps more steps; extension walks
-// still unfinished then are written, with their path and complete walk
-// state, to the launch's carry buffer and their hit word marked -2 (k_shade
-// skips them).  The next bounce launch resumes them first (items 0 .. nC-1,
-// their hits stored after its own extension rays' at nE + k) and its shading
-// kernel shades them at their own depth, one bounce behind the paths around
-// them; the tail kernel takes those of the last bounce launch.  A path's
-// operations keep their order (its connection of the previous bounce was
-// walked before it was carried; every random number is keyed by the path's
-// own depth), so results are unchanged; a launch no longer waits for its few
-// longest walks.
+// warp keeps stepping its walks for carrySteps more steps; walks still
+// unfinished then are written, with their path (or connection) and complete
+// walk state, to the launch's carry buffer, an extension walk's hit word
+// marked -2 (k_shade skips it).  The next bounce launch resumes them after its
+// shadow rays (items nS .. nS+nC-1; their hit words after its own extension
+// rays' at nE + k, -2 for a connection) and its shading kernel shades the
+// extension walks at their own depth, one bounce behind the paths around
+// them; the tail kernel takes those of the last bounce launch.  Results are
+// unchanged: every random number is keyed by the path's own depth, and
+// connections do not add to the slot when their walk ends but store their
+// contribution per bounce, summed in bounce order by k_fold (a path's
+// connections may now finish out of order).  The filter-only mode's bounce-0
+// connections, whose direct-light sample is read by the next bounce's
+// shading, are never carried.
 template <bool kCount, bool kWide>
 __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, RenderBuffers b, int in, int shIn,
                                                               int shReset, uint32_t bilat, uint32_t kRefill,
@@ -521,16 +539,20 @@ __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, Rend
     if (idle == 0xffffffffu && drained) break;
     if constexpr (!kWide) {
       if (carrySteps && drained && in >= 0) {
-        if (dryFor >= carrySteps && has && !any) {
-          const float4* r = prev + (size_t)item * kCarryF4;
-          const bool saved = res ? save_carry(b.carry[launch & 1u], &b.ctr->carryN[launch % 3u], b.carryCap, r,
-                                              r + 1, r + 2, r + 3, w.minT, w.best, w.bu, w.bv, w.bw, w.steps, w.tos,
-                                              w.sp, stack)
-                                 : save_carry(b.carry[launch & 1u], &b.ctr->carryN[launch % 3u], b.carryCap,
-                                              wv.o + item, wv.d + item, wv.thr + item, wv.smp + item, w.minT, w.best,
-                                              w.bu, w.bv, w.bw, w.steps, w.tos, w.sp, stack);
-          if (saved) {
-            b.hit[res ? nE + item : item] = make_float4(-2.f, 0.f, 0.f, 0.f);
+        // once per warp, carrySteps steps after it found the queue empty: its
+        // walks still running take carry records with one atomic for the warp
+        // (walks that find the buffer full finish here)
+        if (dryFor >= carrySteps && dryFor < carrySteps + walk_steps<kWide>()) {
+          const float4* src = res ? prev + (size_t)item * kCarryF4 : (any ? sh + 3 * (size_t)item : wv.o + item);
+          const bool want = has && !(any && bilat && __float_as_uint(src[2].w) == 0u);
+          const uint32_t m = __ballot_sync(0xffffffffu, want);
+          uint32_t c0 = 0;
+          if (m && lane == 0) c0 = atomicAdd(&b.ctr->carryN[launch % 3u], (uint32_t)__popc(m));
+          c0 = __shfl_sync(0xffffffffu, c0, 0) + __popc(m & lanemask_lt());
+          if (want && c0 < b.carryCap) {
+            save_carry(b.carry[launch & 1u] + (size_t)c0 * kCarryF4, src, (res || any) ? 1 : (size_t)(wv.d - wv.o),
+                       any && !res, w.minT, w.best, w.bu, w.bv, w.bw, w.steps, w.tos, w.sp, stack);
+            if (res || !any) b.hit[res ? nE + item : item] = make_float4(-2.f, 0.f, 0.f, 0.f);
             has = false;
           }
         }
@@ -550,11 +572,11 @@ __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, Rend
           any = k < nS;
           res = !any && k < nS + nC;
           item = any ? k : (res ? k - nS : k - nS - nC);
-          if (any) {
+          if (res) {
+            if constexpr (!kWide) any = resume_walk(prev + (size_t)item * kCarryF4, w, stack);
+          } else if (any) {
             const float4 A = sh[3 * (size_t)item], B = sh[3 * (size_t)item + 1];
             w.init(ld3(A), ld3(B), B.w, gb::kBias, stack);
-          } else if (res) {
-            if constexpr (!kWide) resume_walk(prev + (size_t)item * kCarryF4, w, stack);
           } else {
             w.init(ld3(wv.o[item]), ld3(wv.d[item]), gb::kInf, gb::kBias, stack);
           }
@@ -578,14 +600,9 @@ __global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, Rend
       if (fin) {
         has = false;
         if (any) {
-          if (!w.hit()) {  // unoccluded: the connection counts (:716-721)
-            const float4 A = sh[3 * (size_t)item], C = sh[3 * (size_t)item + 2];
-            const uint32_t slot = __float_as_uint(A.w);
-            const float4 r = b.res[slot];
-            b.res[slot] =
-                make_float4(r.x + C.x, r.y + C.y, r.z + C.z, __uint_as_float(__float_as_uint(r.w) + 4u));
-            if (bilat && __float_as_uint(C.w) == 0u) direct_connect(b.dsm, slot, C);  // made at bounce 0
-          }
+          const float4* q = res ? prev + (size_t)item * kCarryF4 : sh + 3 * (size_t)item;
+          if (!w.hit()) connection_reached(b, bilat, q[0], q[2]);  // unoccluded: it counts (:716-721)
+          if (res) b.hit[nE + item] = make_float4(-2.f, 0.f, 0.f, 0.f);
         } else {
           b.hit[res ? nE + item : item] = w.hit() ? make_float4(w.minT, __uint_as_float(w.best), w.bu, w.bv)
                                                   : make_float4(-1.f, 0.f, 0.f, 0.f);
@@ -635,9 +652,8 @@ __device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a
   float pot = io.t.w;  // path potential (filter-only mode)
   if (h4.x < 0.f) {  // miss (:537-542), plus the optional environment term
     if (a.useEnv) pathSample = pathSample + vmul(mk(a.env[0], a.env[1], a.env[2]), outMul);
-    const float4 r = b.res[slot];
-    b.res[slot] = make_float4(r.x + pathSample.x, r.y + pathSample.y, r.z + pathSample.z,
-                              __uint_as_float(__float_as_uint(r.w) + 1u));
+    // the path's end: its emission and how many bounces' connections k_fold sums before it
+    b.res[slot] = make_float4(pathSample.x, pathSample.y, pathSample.z, __uint_as_float(depth));
     if (a.bilat) reinterpret_cast<float*>(b.dsm + slot)[3] = pot;
     if (a.moments) count_path_length(a, b, pix, depth);
     return;
@@ -668,14 +684,13 @@ __device__ __forceinline__ void shade_path(const DevScene& S, const FrameArgs& a
   float contrib = length(outMul) * length(B.lmt);
   if (length(m.emis) > 0.f) contrib = 0.f;
   if (u[6] > contrib || depth + 1 >= a.eyeDepth) {
-    const float4 r = b.res[slot];
-    b.res[slot] = make_float4(r.x + pathSample.x, r.y + pathSample.y, r.z + pathSample.z,
-                              __uint_as_float(__float_as_uint(r.w) + 1u));
+    b.res[slot] = make_float4(pathSample.x, pathSample.y, pathSample.z, __uint_as_float(depth));
     if (a.bilat) reinterpret_cast<float*>(b.dsm + slot)[3] = pot;
     if (a.moments) count_path_length(a, b, pix, depth + 1);
     return;
   }
   io.cont = true;
+  b.conn[(size_t)depth * b.cap + slot] = make_float4(0.f, 0.f, 0.f, 0.f);  // none, until a connection walk says
   outMul = vmul(outMul, B.lmt);
   io.o = st4u(B.nOrig, slot);
   io.d = st4u(B.nDir, pix);
@@ -856,13 +871,21 @@ __global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, Ren
         const uint32_t j = base + __popc(idle & lanemask_lt());
         if (j >= n && j < total) {  // a carried walk: resume it where it stopped
           const float4* r = carried + (size_t)(j - n) * kCarryF4;
-          io.o = r[0];
-          io.d = r[1];
-          io.t = r[2];
-          io.s = r[3];
-          mode = kPathExt;
           resumed = true;
-          if constexpr (!kWide) resume_walk(r, w, stack);
+          if constexpr (!kWide) {
+            if (resume_walk(r, w, stack)) {  // a connection alone, without its path
+              io.shA = r[0];
+              io.shB = r[1];
+              io.shC = r[2];
+              mode = kPathShadow;
+            } else {
+              io.o = r[0];
+              io.d = r[1];
+              io.t = r[2];
+              io.s = r[3];
+              mode = kPathExt;
+            }
+          }
         } else if (j < n) {
           io.o = wv.o[j];
           io.d = wv.d[j];
@@ -892,14 +915,13 @@ __global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, Ren
                     : w.template step<kCount>(S, stack, anyHit, nnE, ntE);
     if (!done) continue;
     if (anyHit) {
-      shRays++;
-      if (!w.hit()) {  // unoccluded connection (:716-721)
-        const uint32_t slot = __float_as_uint(io.shA.w);
-        const float4 r = b.res[slot];
-        b.res[slot] = make_float4(r.x + io.shC.x, r.y + io.shC.y, r.z + io.shC.z,
-                                  __uint_as_float(__float_as_uint(r.w) + 4u));
-        if (a.bilat && __float_as_uint(io.shC.w) == 0u) direct_connect(b.dsm, slot, io.shC);  // made at bounce 0
+      if (!w.hit()) connection_reached(b, a.bilat, io.shA, io.shC);  // unoccluded connection (:716-721)
+      if (resumed) {  // a carried connection alone (counted by its launch): done
+        resumed = false;
+        mode = kIdle;
+        continue;
       }
+      shRays++;
       mode = kPathExt;  // the path's next extension ray
       w.init(ld3(io.o), ld3(io.d), gb::kInf, gb::kBias, stack);
       continue;
@@ -930,6 +952,33 @@ __global__ void __launch_bounds__(kBlock, 3) k_tail(DevScene S, FrameArgs a, Ren
     warp_add_u64(&b.ctr->nodesS, nnS);
     warp_add_u64(&b.ctr->trisS, ntS);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Sum of each path of the band, once all its walks are done: the unoccluded
+// connections of bounces 0 .. k-1 in bounce order, then the path's emission
+// at its end (bounce k), with the count word the accumulation kernels read
+// (4 per connection, 1 for the end): the additions the reference makes into
+// the path's result as each connection and the end happen (:716-721,
+// :520-542), in the same order, so the sums are equal to the bit.
+__global__ void k_fold(RenderBuffers b) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.ctr->paths) return;
+  const uint32_t s = b.base + i;
+  const float4 e = b.res[s];
+  const uint32_t k = min(__float_as_uint(e.w), b.connDepth);
+  float x = 0.f, y = 0.f, z = 0.f;
+  uint32_t n = 0;
+  for (uint32_t d = 0; d < k; d++) {
+    const float4 c = b.conn[(size_t)d * b.cap + s];
+    if (c.w != 0.f) {
+      x = x + c.x;
+      y = y + c.y;
+      z = z + c.z;
+      n += 4u;
+    }
+  }
+  b.res[s] = make_float4(x + e.x, y + e.y, z + e.z, __uint_as_float(n + 1u));
 }
 
 // ---------------------------------------------------------------------------
@@ -1243,6 +1292,13 @@ cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuff
                          bool attach, cudaStream_t st) {
   const uint32_t g = shade_grid();
   k_shade<<<g, kBlock, 0, st>>>(S, a, b, in, launch, attach ? 1u : 0u);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fold(const RenderBuffers& b, cudaStream_t st) {
+  const uint32_t n = b.count ? b.count : b.cap;
+  k_fold<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(b);
   note_launches(1);
   return cudaGetLastError();
 }

@@ -137,6 +137,14 @@ struct RenderBuffers {
   // band, launch L's in buffer L & 1
   float4* carry[2];
   uint32_t carryCap;
+  // per bounce d < connDepth and slot (index d * cap + slot): the connection
+  // the path made at bounce d, contribution.xyz and .w = 1 when its walk found
+  // it unoccluded, 0 when occluded or none was made; k_fold sums them into the
+  // slot's result in bounce order once the frame's walks are done.  Until
+  // then a slot's res word holds the path's emission at its end and, in .w,
+  // the bounce it ended at.
+  float4* conn;
+  uint32_t connDepth;
 };
 constexpr uint32_t kMaxBands = 8;
 constexpr uint32_t kCarryF4 = 14;
@@ -153,6 +161,9 @@ cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffe
 // attach: store each continuing path's connection at the path's index (for the tail kernel)
 cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t launch,
                          bool attach, cudaStream_t st);
+// the sum of every path of the band (connections, then its end): after the
+// band's last walk, before the accumulation
+cudaError_t launch_fold(const RenderBuffers& b, cudaStream_t st);
 // remaining bounces of every path alive at bounce t = min(switch bounce the
 // shading launches recorded, K) when t is below the depth cap (wave t & 1,
 // starting with the connection attached to each path in queue (t - 1) & 1),

@@ -18,6 +18,15 @@ of two frames, where the heuristic's filtered-minus-raw error is still blind).
 
     python tests/experiments/learned_sampler.py --truth DIR [--out report.json]
         [--res 320x180] [--keys 3] [--seconds 0.25,0.5,1,2] [--steps 2000]
+        [--gpu-truth-frames N] [--check-truth]
+
+At 1280x720 the FP64 images are out of reach of the host (the oracle renders
+8192 passes of 320x180 in about 25 minutes on 7 cores; 1280x720 is 16 times
+that per scene), so `--gpu-truth-frames N` renders any missing reference image
+on the GPU instead: N plain-BDPT frames of the same estimator in FP32 with the
+FP64 images' Philox key (777), cached in DIR as gputruth_<seed>_<W>x<H>_<N>.npy.
+`--check-truth` (at a resolution with FP64 images) renders the GPU image too
+and reports its RMSE against the FP64 one beside the errors being compared.
 
 Needs a GPU.  Writes a JSON report and prints a markdown summary.
 """
@@ -81,6 +90,30 @@ def curve(scene, cam, W, H, truth, net, warmup, key, seconds, every=4):
     return pts
 
 
+def truth_image(args, s, W, H):
+    """The scene's reference image: the FP64 one when present, else (with
+    --gpu-truth-frames) a long GPU render with the same Philox key."""
+    fp64 = os.path.join(args.truth, f"truth_{s}_{W}x{H}_{args.truth_frames}.npy")
+    if os.path.exists(fp64):
+        return np.load(fp64).astype(np.float32), "fp64"
+    if not args.gpu_truth_frames:
+        raise SystemExit(f"no reference image {fp64} (render it with make_truth.py, or pass --gpu-truth-frames)")
+    return gpu_truth(args, s, W, H), "gpu"
+
+
+def gpu_truth(args, s, W, H):
+    path = os.path.join(args.truth, f"gputruth_{s}_{W}x{H}_{args.gpu_truth_frames}.npy")
+    if os.path.exists(path):
+        return np.load(path)
+    (v, t, m), cam = learned.hall_scene(s, args.boxes)
+    scene = gb.RTScene(v, t, m).build_bvh()
+    img = learned.converged(gb, scene, cam, W, H, args.gpu_truth_frames, seed=777).astype(np.float32)
+    scene.close()
+    os.makedirs(args.truth, exist_ok=True)
+    np.save(path, img)
+    return img
+
+
 def at(pts, t):
     """RMSE at wall time t (the last point at or before t)."""
     best = pts[0][1]
@@ -112,6 +145,10 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--target-frames", type=int, default=1024)
     ap.add_argument("--learned-warmup", type=int, default=2)
+    ap.add_argument("--gpu-truth-frames", type=int, default=0,
+                    help="render missing reference images on the GPU with this many frames")
+    ap.add_argument("--check-truth", action="store_true",
+                    help="also render the GPU reference where an FP64 one exists and compare the two")
     args = ap.parse_args()
     W, H = (int(x) for x in args.res.split("x"))
     secs = [float(x) for x in args.seconds.split(",")]
@@ -126,9 +163,13 @@ def main():
     # its own tile feature (log of the tile's mean filtered-minus-raw error)
     A = np.stack([X[:, 22], np.ones(len(X))], 1)
     coef = np.linalg.lstsq(A, Y, rcond=None)[0]
-    rows, pred_rows = [], []
+    rows, pred_rows, truth_rows = [], [], []
     for s in seeds(args.test_seeds):
-        truth = np.load(os.path.join(args.truth, f"truth_{s}_{W}x{H}_{args.truth_frames}.npy")).astype(np.float32)
+        truth, kind = truth_image(args, s, W, H)
+        if args.check_truth and kind == "fp64" and args.gpu_truth_frames:
+            g = gpu_truth(args, s, W, H)
+            truth_rows.append(dict(seed=s, gpu_vs_fp64_rmse=float(np.sqrt(np.mean((g.astype(np.float64) - truth) ** 2))),
+                                   fp64_mean=float(truth.mean())))
         (v, t, m), cam = learned.hall_scene(s, args.boxes)
         scene = gb.RTScene(v, t, m).build_bvh()
         r = gb.RTRenderer(W, H, layouts.MODE_BDPT_SC_ADAP_BILAT,
@@ -148,7 +189,7 @@ def main():
         for key in range(args.keys):
             plain = curve(scene, cam, W, H, truth, None, 5, key, max(secs))
             lrn = curve(scene, cam, W, H, truth, net, args.learned_warmup, key, max(secs))
-            row = dict(seed=s, key=key)
+            row = dict(seed=s, key=key, truth=kind)
             for sec in secs:
                 ep, el = at(plain, sec), at(lrn, sec)
                 tt = time_to(lrn, ep)
@@ -169,12 +210,15 @@ def main():
                keys=args.keys, samples=int(len(X)), steps=args.steps, target_frames=args.target_frames,
                truth_frames=args.truth_frames, learned_warmup=args.learned_warmup,
                loss_first=float(losses[:10].mean()), loss_last=float(losses[-10:].mean()), data_seconds=t_data,
-               train_seconds=t_train, summary=summ, rows=rows, tile_prediction=pred_rows,
+               train_seconds=t_train, summary=summ, rows=rows, tile_prediction=pred_rows, truth_check=truth_rows,
+               gpu_truth_frames=args.gpu_truth_frames,
                tile_prediction_mse=dict(network=float(np.mean([p["network"] for p in pred_rows])),
                                         heuristic=float(np.mean([p["heuristic"] for p in pred_rows])),
                                         constant=float(np.mean([p["constant"] for p in pred_rows]))))
     with open(args.out, "w") as f:
         json.dump(rep, f, indent=1)
+    for tr in truth_rows:
+        print(f"seed {tr['seed']}: GPU reference vs FP64 reference RMSE {tr['gpu_vs_fp64_rmse']:.5f}")
     tp = rep["tile_prediction_mse"]
     print(f"held-out tile log-error prediction MSE: network {tp['network']:.4f}, heuristic line "
           f"{tp['heuristic']:.4f}, constant {tp['constant']:.4f}")

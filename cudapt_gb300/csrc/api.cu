@@ -475,7 +475,7 @@ uint64_t gbpt::renderer_bytes(uint32_t W, uint32_t H, const gbpt_params& p) {
   const size_t np = (size_t)W * H;
   const uint32_t cacheCap = std::max(1u, p.light_paths * (1 + p.light_depth_max));
   return np * (128 + 16 + 96 + 16 + 48 + 16 + 8) + np * (12 * 10 + 4 * 2 + 4 * 5) + (size_t)cacheCap * 192 +
-         std::max<size_t>(np / 8, 256) * (2 * kCarryF4 + 1) * 16 +
+         std::max<size_t>(std::min<size_t>(np, walk_lanes()), 256) * (2 * kCarryF4 + 1) * 16 +
          np * 16 * (std::max(std::max(p.eye_depth_max, p.pt_depth_max), 2u) - 1);
 }
 
@@ -498,9 +498,11 @@ gbpt_status ensure_alloc(gbpt_renderer* r) {
     float4* b = r->waveMem + (size_t)k * 4 * cap;
     r->rb.wave[k] = Wave{b, b + cap, b + 2 * cap, b + 3 * cap};
   }
-  // hit words: one per live path of the wave, plus one per walk a launch
-  // resumes (carried connection walks are not paths: they take words past the paths')
-  r->rb.carryCap = (uint32_t)std::max<size_t>(cap / 8, 256);
+  // carry records: as many as the walk grid has lanes (a launch carries at
+  // most one walk per lane), but no more than paths.  Hit words: one per live
+  // path of the wave, plus one per walk a launch resumes (carried connection
+  // walks are not paths: they take words past the paths').
+  r->rb.carryCap = (uint32_t)std::max<size_t>(std::min<size_t>(cap, walk_lanes()), 256);
   CK(dalloc(&r->rb.hit, cap + r->rb.carryCap));
   CK(dalloc(&r->rb.sh[0], cap * 3));
   CK(dalloc(&r->rb.sh[1], cap * 3));

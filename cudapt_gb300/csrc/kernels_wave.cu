@@ -1252,6 +1252,8 @@ cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffe
   return cudaGetLastError();
 }
 
+uint32_t walk_lanes() { return walk_grid<false, false>() * (uint32_t)kBlock; }
+
 void prepare_launches() {
   walk_grid<false, false>();
   walk_grid<false, true>();

@@ -161,6 +161,8 @@ cudaError_t launch_walk(const DevScene& S, const FrameArgs& a, const RenderBuffe
 // attach: store each continuing path's connection at the path's index (for the tail kernel)
 cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t launch,
                          bool attach, cudaStream_t st);
+// threads of the persistent walk grid (the most walks one launch can carry)
+uint32_t walk_lanes();
 // the sum of every path of the band (connections, then its end): after the
 // band's last walk, before the accumulation
 cudaError_t launch_fold(const RenderBuffers& b, cudaStream_t st);

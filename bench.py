@@ -57,7 +57,7 @@ WORKLOADS = {
 }
 
 # static per-ray issue figures of the walk kernels, from single-kernel ncu captures
-ISSUE_PROFILES = {"hall": "profiles/k_walk_hall_640x360.md", "interior": "profiles/k_walk_k_tail_interior_512x384.md"}
+ISSUE_PROFILES = {"hall": "profiles/k_walk_k_tail_hall_640x360.md", "interior": "profiles/k_walk_k_tail_interior_512x384.md"}
 SMS, SCHEDULERS = 152, 4
 
 
@@ -432,7 +432,7 @@ def bench_gpu(args, wl):
                     "so DRAM carries a small part of these bytes and the issue side below is the real limit",
             "algorithmic_bytes_per_frame": int(trace_bytes),
             "traffic": int(prof["dram_bytes_per_path"] * np_) if "dram_bytes_per_path" in prof else None,
-            "traffic_source": (f"{prof_src} (static: DRAM bytes per camera path of one frame's walk launches in an "
+            "traffic_source": (f"{prof_src} (static: DRAM bytes per camera path of one frame's walk and tail launches in an "
                                f"ncu capture of a smaller frame of the same scene, times this frame's paths)")
             if "dram_bytes_per_path" in prof else None,
             "l2_bytes_per_frame": int(prof["l2_bytes_per_path"] * np_) if "l2_bytes_per_path" in prof else None,

@@ -68,12 +68,16 @@ def converged(gb, scene, cam, width, height, frames, depth=5, seed=1234):
     return img
 
 
-def samples_for_scene(gb, seed, width=320, height=180, snapshots=(5, 7, 10, 14), conv_frames=512, boxes=300):
-    """(features, targets) of one training scene at several points of a plain adaptive run."""
+def samples_for_scene(gb, seed, width=320, height=180, snapshots=(5, 7, 10, 14), conv_frames=512, boxes=300,
+                      warmup=5):
+    """(features, targets) of one training scene at several points of a plain
+    adaptive run (budgeted frames after `warmup` uniform ones); the targets'
+    converged image has its own Philox key (999), so it shares no samples
+    with the run it scores."""
     (v, t, m), cam = hall_scene(seed, boxes)
     scene = gb.RTScene(v, t, m).build_bvh()
-    ref = converged(gb, scene, cam, width, height, conv_frames)
-    r = gb.RTRenderer(width, height, layouts.MODE_BDPT_SC_ADAP_BILAT, adaptive_params())
+    ref = converged(gb, scene, cam, width, height, conv_frames, seed=999)
+    r = gb.RTRenderer(width, height, layouts.MODE_BDPT_SC_ADAP_BILAT, adaptive_params(warmup_frames=warmup))
     r.set_mlp(None, collect=True)
     X, Y = [], []
     for f in range(1, max(snapshots) + 1):

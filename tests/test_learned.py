@@ -109,16 +109,27 @@ def test_gpu_learned_allocation_renders_same_image(gbdev):
 
 @pytest.mark.gpu
 def test_gpu_training_on_rendered_tiles(gbdev):
-    """Samples from two small hall scenes: the trained network predicts the
-    held-out scene's tile errors better than a constant."""
+    """Samples from three small hall scenes: the trained network predicts a
+    held-out scene's tile errors better than a constant and better than the
+    plain heuristic's own tile error (a least-squares line on that feature,
+    fitted to the same training tiles).  The equal-time RMSE of the learned
+    allocation itself does not beat the plain allocator on these scenes
+    (tests/experiments/learned_sampler.py), so no test asserts that."""
     Xs, Ys = [], []
-    for seed in (1, 2, 21):
-        X, Y = learned.samples_for_scene(gbdev, seed, width=128, height=72, snapshots=(5, 8), conv_frames=128,
-                                         boxes=60)
+    for seed in (1, 2, 3, 21):
+        X, Y = learned.samples_for_scene(gbdev, seed, width=160, height=96, snapshots=(2, 5, 8), conv_frames=256,
+                                         boxes=120, warmup=2)
         Xs.append(X)
         Ys.append(Y)
-    net, losses = learned.train(np.concatenate(Xs[:2]), np.concatenate(Ys[:2]), steps=300, batch=1024, lr=3e-3)
+    Xt, Yt = np.concatenate(Xs[:3]), np.concatenate(Ys[:3])
+    net, losses = learned.train(Xt, Yt, steps=600, batch=1024, lr=3e-3)
     assert losses[-20:].mean() < 0.7 * losses[:5].mean()
-    pred = net.forward(Xs[2])
+    pred = net.forward(Xs[3])
     pred -= pred.mean()
-    assert np.mean((pred - Ys[2]) ** 2) < 0.9 * np.mean(Ys[2] ** 2)
+    A = np.stack([Xt[:, 22], np.ones(len(Xt))], 1)
+    coef = np.linalg.lstsq(A, Yt, rcond=None)[0]
+    line = np.stack([Xs[3][:, 22], np.ones(len(Xs[3]))], 1) @ coef
+    line -= line.mean()
+    mse_net, mse_line, mse_const = (float(np.mean((x - Ys[3]) ** 2)) for x in (pred, line, 0.0))
+    assert mse_net < 0.9 * mse_const, (mse_net, mse_const)
+    assert mse_net < mse_line, (mse_net, mse_line)

@@ -6,20 +6,25 @@
 //   light pass (1 CTA)          pt_genLightPathQueue_kernel + pt_traceLight_kernel
 //                               loop with stable compaction (:875-906)
 //   camera                      pt_genPathQueue_kernel (:619-640)
-//   per bounce d:
-//     trace  (closest hit)      the TracePrimitive half of pt_traceSample_kernel
+//   per bounce launch d (k_walk, then k_shade):
+//     shadow (any hit)          the visibility test of GetLightFromRandLightVertices
+//                               (:665-700) for bounce d-1's connections
+//     trace  (closest hit)      the TracePrimitive half of pt_traceSample_kernel,
+//                               for the walks launch d-1 carried and wave d
 //     shade                     the rest of pt_traceSample_kernel (:365-543);
 //                               survivors are appended to the other wave
 //                               buffer with one atomic per warp (replaces
 //                               thrust::remove_if, :930), connection requests
 //                               likewise (replaces thrust::copy_if, :934)
-//     shadow (any hit)          the visibility test of GetLightFromRandLightVertices
-//                               (:665-700) and the accumulate of
-//                               pt_connectEyeLightPath_kernel (:703-723)
+//   tail (k_tail)               the remaining bounces of the paths still alive,
+//                               one lane per path, and the last launch's carried walks
+//   fold (k_fold)               the accumulate of pt_connectEyeLightPath_kernel
+//                               (:703-723) and of the path's end, in bounce order
 //   apply                       pt_applyPathQueueResult_kernel (:741-778)
 //
 // Queue lengths live in device memory (DevCounters) and every kernel runs a
-// grid-stride loop over them, so the host never waits on a count.
+// grid-stride loop or a persistent fetch loop over them, so the host never
+// waits on a count.
 #include <algorithm>
 #include <atomic>
 #include <cuda_runtime.h>

@@ -343,6 +343,27 @@ __global__ void __launch_bounds__(1024) k_light(DevScene S, FrameArgs a, float4*
 // Camera rays, one per pixel (pt_genPathQueue_kernel, :619-640), for the
 // band's pixels b.base .. b.base + b.count - 1; a ray's wave index is its
 // index inside the band.
+// Wave item i of a whole-image wavefront -> its pixel: 4x8-pixel tiles, one
+// warp's 32 camera rays per tile, tiles in row-major order, then the pixels
+// right of and below the whole tiles in row-major order (a bijection for any
+// width and height).  Camera rays of a compact tile walk more of the same
+// nodes than a 32-pixel row: hall 1280x720 188.0 -> 190.1 Mpaths/s (8x4
+// tiles 189.2, 16x2 187.8; interior and Cornell within noise).  Results do not
+// depend on it: every path's random numbers and its slot follow from its pixel.
+__device__ __forceinline__ uint32_t tiled_pixel(uint32_t i, uint32_t w, uint32_t h) {
+  constexpr uint32_t TW = 4u, TH = 8u;
+  const uint32_t tx = w / TW, ty = h / TH, nFull = tx * ty * TW * TH;
+  if (i < nFull) {
+    const uint32_t t = i / (TW * TH), k = i % (TW * TH);
+    return ((t / tx) * TH + k / TW) * w + (t % tx) * TW + k % TW;
+  }
+  uint32_t j = i - nFull;
+  const uint32_t rw = w - tx * TW, rightN = rw * ty * TH;
+  if (j < rightN) return (j / rw) * w + tx * TW + j % rw;
+  j -= rightN;
+  return (ty * TH + j / w) * w + j % w;
+}
+
 __global__ void k_camera(FrameArgs a, RenderBuffers b) {
   using namespace gb;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -355,7 +376,8 @@ __global__ void k_camera(FrameArgs a, RenderBuffers b) {
     b.ctr->tailAt = 0xFFFFFFFFu;
   }
   if (i >= b.count) return;
-  const uint32_t p = b.base + i;
+  // local pixel (the band's range in row-major order when the frame is split)
+  const uint32_t p = b.count == a.width * a.height ? tiled_pixel(i, a.width, a.height) : b.base + i;
   // pixel of the full image: its coordinates place the ray and its id keys
   // every random number of the path, so a window renders as in the full image
   const uint32_t x = a.winX0 + p % a.width, y = a.winY0 + p / a.width;

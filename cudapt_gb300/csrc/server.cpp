@@ -82,16 +82,18 @@ struct Knobs {
 // large workloads (small images favour earlier refills and earlier tails,
 // whose per-bounce launches wait on their slowest ray), then launch shapes:
 // persistent grids of 2 or 3 CTAs per SM, which leave SMs to the requests
-// running beside, two bands for images of 512K pixels and more, and the tail
-// switch decided on the device at two live-path fractions.
+// running beside, and the tail switch decided on the device at two
+// live-path fractions.  (Two bands, once a candidate for images of 512K
+// pixels and more, measured 7-9 % slower than one band since walks are
+// carried between launches.)
 std::vector<Knobs> candidates(uint32_t depth, uint32_t sizeLog2, float below) {
+  (void)sizeLog2;
   std::vector<Knobs> c = {{8, -1, 1, 0, below}, {4, -1, 1, 0, below}, {16, -1, 1, 0, below}};
   if (depth > 3) c.push_back({8, (int32_t)depth - 3, 1, 0, below});
   if (depth > 5) c.push_back({8, (int32_t)depth - 5, 1, 0, below});
   c.push_back({8, (int32_t)depth, 1, 0, 0.f});  // no tail kernel but the carried walks'
   c.push_back({8, -1, 1, 2, below});
   c.push_back({8, -1, 1, 3, below});
-  if (sizeLog2 >= 19) c.push_back({8, -1, 2, 0, below});
   for (float f : {0.25f, 0.5f})
     if (f != below) c.push_back({8, (int32_t)depth, 1, 0, f});
   return c;

@@ -348,8 +348,10 @@ __global__ void __launch_bounds__(1024) k_light(DevScene S, FrameArgs a, float4*
 // right of and below the whole tiles in row-major order (a bijection for any
 // width and height).  Camera rays of a compact tile walk more of the same
 // nodes than a 32-pixel row: hall 1280x720 188.0 -> 190.1 Mpaths/s (8x4
-// tiles 189.2, 16x2 187.8; interior and Cornell within noise).  Results do not
-// depend on it: every path's random numbers and its slot follow from its pixel.
+// tiles 189.2, 16x2 187.8), interior even, Cornell 256x256 190.1 -> 187.2
+// (cheap walks: its first-bounce slot writes in 4-pixel runs show).  Results
+// do not depend on it: every path's random numbers and its slot follow from
+// its pixel.
 __device__ __forceinline__ uint32_t tiled_pixel(uint32_t i, uint32_t w, uint32_t h) {
   constexpr uint32_t TW = 4u, TH = 8u;
   const uint32_t tx = w / TW, ty = h / TH, nFull = tx * ty * TW * TH;

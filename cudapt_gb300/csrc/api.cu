@@ -801,7 +801,9 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
     const uint32_t D = a.eyeDepth;
     const bool wideT = S.traversal == 1 && S.wide;
     const bool carrying = a.carrySteps && !wideT;
-    const uint32_t K = std::min(tail_from(D, wideT, r->p.tail_from), D);
+    const size_t np = (size_t)r->W * r->H;
+    const uint32_t nb = adaptive ? 1u : bands_for(r->p.bands, np, carrying);
+    const uint32_t K = std::min(tail_from(D, wideT, r->p.tail_from, np / nb, carrying), D);
     const bool tailRun = K < D || carrying || a.tailBelow > 0.f;
     auto bounces = [&](const RenderBuffers& rbx, cudaStream_t sx, bool mk) -> gbpt_status {
       int in = 0;
@@ -822,8 +824,6 @@ gbpt_status frame_once(gbpt_renderer* r, gbpt_scene* s, const gbpt_camera* cam, 
       CK(launch_fold(rbx, sx));
       return GBPT_OK;
     };
-    const size_t np = (size_t)r->W * r->H;
-    const uint32_t nb = adaptive ? 1u : bands_for(r->p.bands, np, carrying);
     r->lastBands = nb;
     if (budgeted || nb == 1) {
       if (!budgeted) {

@@ -1295,8 +1295,19 @@ void prepare_launches() {
   shade_grid();
 }
 
-uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested) {
-  // default when D > 6: the tail kernel from bounce D/2 - 1 in the reference
+uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested, size_t paths, bool carrying) {
+  // default while carrying (reference order): a frame with fewer camera paths
+  // than the walk grid has lanes hands its paths to the tail kernel from bounce
+  // 2 on, a larger one from bounce D/2 when D > 6, else never.  Measured with
+  // carrying (Mpaths/s): Cornell 256x256 (65,536 paths against 194,560 lanes),
+  // D = 8: from 2 204.6, 3 193.6, 4 180.6, 5 168.2; interior 1024x768, D = 10:
+  // from 3 163.0, 4 167.5, 5 170.6, 6 169.7; hall 1280x720, D = 5: none 188.1
+  // (launches past the cap: worse).  Against the rule without carrying: interior
+  // 168.4 -> 172.3, Cornell 188.9 -> 194.6, hall and hall adaptive even.  The
+  // same choice on the device (a shading launch switching once the live paths
+  // fall below 1-3 x the lanes) cost Cornell 14 %: the host still issues the
+  // skipped launches.
+  // default without carrying, D > 6: from bounce D/2 - 1 in the reference
   // order, D/2 in the wide order; per-bounce launches throughout for D <= 6.
   // Measured in Mpaths/s (reference / wide order), tail kernel at three CTAs
   // per SM: interior, D = 10: from 4 174.3 / 169.6, from 5 170.6 / 174.8,
@@ -1309,6 +1320,10 @@ uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested) {
     return e ? std::atoi(e) : -2;
   }();
   if (requested >= 0) return (uint32_t)requested;
+  if (v == -2 && carrying) {
+    if (paths < walk_lanes()) return std::min(eyeDepth, 2u);
+    return eyeDepth > 6 ? eyeDepth / 2 : eyeDepth;
+  }
   if (v == -2) return eyeDepth > 6 ? eyeDepth / 2 - (wide ? 0u : 1u) : eyeDepth;
   return v < 0 ? eyeDepth : (uint32_t)v;
 }

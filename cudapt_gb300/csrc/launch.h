@@ -174,7 +174,10 @@ cudaError_t launch_tail(const DevScene& S, const FrameArgs& a, const RenderBuffe
 // first bounce handled by the tail kernel: `requested` when >= 0 (>= D: none),
 // else GBPT_TAIL_FROM when set, else D/2 - 1 (wide order: D/2) for D > 6 and
 // none for D <= 6
-uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested);
+// first bounce the tail kernel carries (requested >= 0, the GBPT_TAIL_FROM
+// override, or the default for the depth cap, the paths of one wavefront and
+// whether the bounce launches carry walks)
+uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested, size_t paths, bool carrying);
 // refill threshold of the persistent walks: `requested` when 1..32, else
 // GBPT_WALK_REFILL when set, else 8 (reference order) or 20 (wide order)
 uint32_t walk_refill_for(uint32_t requested, bool wide);

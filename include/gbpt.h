@@ -104,7 +104,10 @@ typedef struct gbpt_params {
   uint32_t walk_refill;     /* idle lanes of a warp that make a persistent walk fetch new rays
                                (1..32; 0: 8 in the reference order, 20 in the wide order) */
   int32_t tail_from;        /* first bounce the per-path tail kernel carries (>= the depth cap: none;
-                               -1: depth / 2 - 1 (wide order: depth / 2) when the cap exceeds 6, else none) */
+                               -1: while carrying, bounce 2 for a frame with fewer camera paths than the
+                               walk grid has lanes, else depth / 2 when the cap exceeds 6, else none;
+                               without carrying depth / 2 - 1 (wide order: depth / 2) when the cap
+                               exceeds 6, else none) */
   uint32_t bands;           /* wavefronts a frame's camera paths are split into, each on its own stream
                                (1..8; 0: 1 while carry_steps is on, else 2 from 512K paths, else 1); the
                                adaptive modes use 1 */

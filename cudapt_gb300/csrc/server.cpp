@@ -78,9 +78,9 @@ struct Knobs {
 
 // Candidates per class: the library default first (one band: concurrent
 // requests already overlap each other's walks), then the refill thresholds
-// and wavefront depths around it that measured within a few percent on the
-// large workloads (small images favour earlier refills and earlier tails,
-// whose per-bounce launches wait on their slowest ray), then launch shapes:
+// and tail starts around it that measured within a few percent on the
+// large workloads (small images favour earlier refills and earlier tails;
+// a frame near the walk grid's size can go either way), then launch shapes:
 // persistent grids of 2 or 3 CTAs per SM, which leave SMs to the requests
 // running beside, and the tail switch decided on the device at two
 // live-path fractions.  (Two bands, once a candidate for images of 512K
@@ -88,14 +88,22 @@ struct Knobs {
 // carried between launches.)
 std::vector<Knobs> candidates(uint32_t depth, uint32_t sizeLog2, float below) {
   (void)sizeLog2;
-  std::vector<Knobs> c = {{8, -1, 1, 0, below}, {4, -1, 1, 0, below}, {16, -1, 1, 0, below}};
-  if (depth > 3) c.push_back({8, (int32_t)depth - 3, 1, 0, below});
-  if (depth > 5) c.push_back({8, (int32_t)depth - 5, 1, 0, below});
-  c.push_back({8, (int32_t)depth, 1, 0, 0.f});  // no tail kernel but the carried walks'
-  c.push_back({8, -1, 1, 2, below});
-  c.push_back({8, -1, 1, 3, below});
+  std::vector<Knobs> c;
+  auto add = [&](Knobs k) {
+    if (std::find(c.begin(), c.end(), k) == c.end()) c.push_back(k);
+  };
+  add({8, -1, 1, 0, below});
+  add({4, -1, 1, 0, below});
+  add({16, -1, 1, 0, below});
+  if (depth > 3) add({8, (int32_t)depth - 3, 1, 0, below});
+  if (depth > 5) add({8, (int32_t)depth - 5, 1, 0, below});
+  if (depth > 6) add({8, (int32_t)depth / 2 - 1, 1, 0, below});
+  if (depth > 2) add({8, 2, 1, 0, below});  // the default for frames smaller than the walk grid
+  add({8, (int32_t)depth, 1, 0, 0.f});  // no tail kernel but the carried walks'
+  add({8, -1, 1, 2, below});
+  add({8, -1, 1, 3, below});
   for (float f : {0.25f, 0.5f})
-    if (f != below) c.push_back({8, (int32_t)depth, 1, 0, f});
+    if (f != below) add({8, (int32_t)depth, 1, 0, f});
   return c;
 }
 

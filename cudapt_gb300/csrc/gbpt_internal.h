@@ -36,6 +36,8 @@ gbpt_status mlp_forward_async(gbpt_mlp* m, const float* x, uint32_t n, float* y,
 
 // device bytes a renderer of this size allocates (its admission figure)
 uint64_t renderer_bytes(uint32_t W, uint32_t H, const gbpt_params& p);
+// the walks' refill threshold for a requested value (0: the library's default)
+uint32_t walk_refill_for(uint32_t requested, bool wide);
 
 // thread-local error text (gbpt_last_error_string)
 void set_error(const std::string& s);

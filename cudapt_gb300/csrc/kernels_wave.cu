@@ -447,12 +447,16 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, uint32_t v
 // 1-2% faster than 4 or 6 on the interior and hall workloads; 4 for the wide
 // walk (its wide-node step needs more registers).
 // walk steps per refill check (measured in Mpaths/s on interior / hall /
-// Cornell): reference order 1: 148.4 / 167.6 / 140.7, 2: 152.2 / 171.7 /
-// 144.5, 4: 154.9 / 174.3 / 143.1, 6: 156.0 / 176.2 / 141.9, 8: 155.5 /
-// 176.6 / 142.7; wide order 2: 170.0 / 180.7 / 159.2, 4: 171.2 / 181.8 / 157.4
+// Cornell): reference order before carrying 1: 148.4 / 167.6 / 140.7, 2:
+// 152.2 / 171.7 / 144.5, 4: 154.9 / 174.3 / 143.1, 6: 156.0 / 176.2 / 141.9,
+// 8: 155.5 / 176.6 / 142.7; with carrying (a launch's end no longer waits on
+// idle lanes) and refill at 2 idle lanes: hall / interior / hall adaptive 6
+// (refill 8): 190.0 / 172.3 / 147.4, 12: 195.1 / 177.8 / 150.9, 16: 196.5 /
+// 178.1 / 151.3, 24 (refill 4): 195.2 / 178.3 / 151.4; wide order 2: 170.0 /
+// 180.7 / 159.2, 4: 171.2 / 181.8 / 157.4
 template <bool kWide>
 __host__ __device__ constexpr int walk_steps() {
-  return kWide ? 2 : 6;
+  return kWide ? 2 : 16;
 }
 
 // Word 3.w of a carry record: the path's depth for an extension walk, this
@@ -1331,7 +1335,7 @@ uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested, size_t paths
 uint32_t walk_refill_for(uint32_t requested, bool wide) {
   if (requested >= 1 && requested <= 32) return requested;
   if (walk_refill_env()) return walk_refill_env();
-  return wide ? 20u : 8u;
+  return wide ? 20u : 2u;
 }
 
 cudaError_t launch_shade(const DevScene& S, const FrameArgs& a, const RenderBuffers& b, int in, uint32_t launch,

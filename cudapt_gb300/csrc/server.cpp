@@ -92,18 +92,19 @@ std::vector<Knobs> candidates(uint32_t depth, uint32_t sizeLog2, float below) {
   auto add = [&](Knobs k) {
     if (std::find(c.begin(), c.end(), k) == c.end()) c.push_back(k);
   };
-  add({8, -1, 1, 0, below});
+  const uint32_t rf = walk_refill_for(0, false);  // the library's refill threshold
+  add({rf, -1, 1, 0, below});
   add({4, -1, 1, 0, below});
-  add({16, -1, 1, 0, below});
-  if (depth > 3) add({8, (int32_t)depth - 3, 1, 0, below});
-  if (depth > 5) add({8, (int32_t)depth - 5, 1, 0, below});
-  if (depth > 6) add({8, (int32_t)depth / 2 - 1, 1, 0, below});
-  if (depth > 2) add({8, 2, 1, 0, below});  // the default for frames smaller than the walk grid
-  add({8, (int32_t)depth, 1, 0, 0.f});  // no tail kernel but the carried walks'
-  add({8, -1, 1, 2, below});
-  add({8, -1, 1, 3, below});
+  add({8, -1, 1, 0, below});
+  if (depth > 3) add({rf, (int32_t)depth - 3, 1, 0, below});
+  if (depth > 5) add({rf, (int32_t)depth - 5, 1, 0, below});
+  if (depth > 6) add({rf, (int32_t)depth / 2 - 1, 1, 0, below});
+  if (depth > 2) add({rf, 2, 1, 0, below});  // the default for frames smaller than the walk grid
+  add({rf, (int32_t)depth, 1, 0, 0.f});  // no tail kernel but the carried walks'
+  add({rf, -1, 1, 2, below});
+  add({rf, -1, 1, 3, below});
   for (float f : {0.25f, 0.5f})
-    if (f != below) add({8, (int32_t)depth, 1, 0, f});
+    if (f != below) add({rf, (int32_t)depth, 1, 0, f});
   return c;
 }
 
@@ -510,7 +511,7 @@ gbpt_status gbpt_server_tuned(gbpt_server* s, int32_t mode, uint32_t depth, uint
   std::lock_guard<std::mutex> lock(s->mu);
   auto it = s->tuning.find(ClassKey{mode, depth, probe.size()});
   if (it == s->tuning.end()) {
-    *walk_refill = 8;
+    *walk_refill = walk_refill_for(0, false);
     *tail_from = -1;
     *samples = 0;
     return GBPT_OK;

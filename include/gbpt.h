@@ -102,7 +102,7 @@ typedef struct gbpt_params {
   uint32_t pt_depth_max;    /* "PTSC" bounce cap, NORMALRAY_BOUND_MAX of src/cudaRTPTStream.cu:6 (10) */
   /* scheduling of the wavefront (results do not depend on either) */
   uint32_t walk_refill;     /* idle lanes of a warp that make a persistent walk fetch new rays
-                               (1..32; 0: 8 in the reference order, 20 in the wide order) */
+                               (1..32; 0: 2 in the reference order, 20 in the wide order) */
   int32_t tail_from;        /* first bounce the per-path tail kernel carries (>= the depth cap: none;
                                -1: while carrying, bounce 2 for a frame with fewer camera paths than the
                                walk grid has lanes, else depth / 2 when the cap exceeds 6, else none;

@@ -443,9 +443,12 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, uint32_t v
 // results do not depend on this scheduling.  The any-hit walk stops at the
 // first hit closer than maxDist: that is exactly when the reference's
 // closest-hit walk with the same maxDist would report a hit.
-// 5 resident CTAs per SM (48 registers) for the reference order: measured
-// 1-2% faster than 4 or 6 on the interior and hall workloads; 4 for the wide
-// walk (its wide-node step needs more registers).
+// 4 resident CTAs per SM (64 registers, no spill) for both orders.  The
+// reference order measured 1-2% faster at 5 (48 registers) than at 4 or 6
+// before walks were carried and before 16-step batches; now (hall / interior
+// / Cornell / hall adaptive, Mpaths/s) 3: 173.2 / 160.6 / 204.5 / 137.8, 4:
+// 198.7 / 179.9 / 198.5 / 153.8, 5: 196.0 / 178.5 / 190.4 / 151.6, 6: 180.9 /
+// 168.0 / 187.3 / 141.1.
 // walk steps per refill check (measured in Mpaths/s on interior / hall /
 // Cornell): reference order before carrying 1: 148.4 / 167.6 / 140.7, 2:
 // 152.2 / 171.7 / 144.5, 4: 154.9 / 174.3 / 143.1, 6: 156.0 / 176.2 / 141.9,
@@ -541,7 +544,7 @@ __device__ __forceinline__ uint32_t carried_of(const RenderBuffers& b, uint32_t 
 // connections, whose direct-light sample is read by the next bounce's
 // shading, are never carried.
 template <bool kCount, bool kWide>
-__global__ void __launch_bounds__(kBlock, kWide ? 4 : 5) k_walk(DevScene S, RenderBuffers b, int in, int shIn,
+__global__ void __launch_bounds__(kBlock, 4) k_walk(DevScene S, RenderBuffers b, int in, int shIn,
                                                               int shReset, uint32_t bilat, uint32_t kRefill,
                                                               uint32_t launch, uint32_t carrySteps) {
   if (b.ctr->tailAt <= launch) return;  // the frame's tail kernel carries this bounce
@@ -1303,7 +1306,8 @@ uint32_t tail_from(uint32_t eyeDepth, bool wide, int32_t requested, size_t paths
   // default while carrying (reference order): a frame with fewer camera paths
   // than the walk grid has lanes hands its paths to the tail kernel from bounce
   // 2 on, a larger one from bounce D/2 when D > 6, else never.  Measured with
-  // carrying (Mpaths/s): Cornell 256x256 (65,536 paths against 194,560 lanes),
+  // carrying (Mpaths/s; the walk grid then had 194,560 lanes, now 155,648):
+  // Cornell 256x256 (65,536 paths),
   // D = 8: from 2 204.6, 3 193.6, 4 180.6, 5 168.2; interior 1024x768, D = 10:
   // from 3 163.0, 4 167.5, 5 170.6, 6 169.7; hall 1280x720, D = 5: none 188.1
   // (launches past the cap: worse).  Against the rule without carrying: interior

@@ -265,22 +265,32 @@ def test_mode_switch_and_result_buffers(gbdev):
     img[:] = 0  # still valid memory after the release
 
 
-@pytest.mark.parametrize("name,W,H,depth", [("interior", 1024, 768, 10), ("hall", 1280, 720, 5)])
-def test_full_size_frame_bands_match_oracle(gbdev, orc, name, W, H, depth):
+@pytest.mark.parametrize("name,W,H,depth,mode,extra", [
+    ("interior", 1024, 768, 10, 0, {}),
+    ("interior", 1024, 768, 10, 0, dict(level=3, env=(0.1, 0.1, 0.1))),  # the benchmark interior as stated
+    ("hall", 1280, 720, 5, 0, {}),
+    ("hall", 1280, 720, 8, 4, {}),  # unidirectional PTSC on the hall
+])
+def test_full_size_frame_bands_match_oracle(gbdev, orc, name, W, H, depth, mode, extra):
     """The benchmark workloads at full size: one GPU frame against the
     oracle's rendering of three 4-row bands of the same frame (every path's
     random numbers follow from its global pixel id and the frame's light
     cache, so a window of the image renders alone)."""
     from cudapt_gb300 import scenes
-    (v, t, m), cam = getattr(scenes, name)()
-    params = gbdev.default_params(eye_depth_max=depth, light_depth_max=depth)
+    extra = dict(extra)
+    env = extra.pop("env", None)
+    (v, t, m), cam = getattr(scenes, name)(**extra)
+    pk = dict(eye_depth_max=depth, light_depth_max=depth, pt_depth_max=depth)
+    if env is not None:
+        pk["env"] = env
+    params = gbdev.default_params(**pk)
     s = gbdev.RTScene(v, t, m).build_bvh()
-    r = gbdev.RTRenderer(W, H, 0, params)
+    r = gbdev.RTRenderer(W, H, mode, params)
     img = r.render(s, cam).reshape(H, W, 3).copy()
     assert r.last_stats["paths"] == W * H
     osc = orc.Scene(v, t, m)
     for y0 in (0, H // 2, H - 4):
-        ref = orc.Renderer(W, 4, 0, params)
+        ref = orc.Renderer(W, 4, mode, params)
         ref.set_window(0, y0, W, H)
         ref.render(osc, cam, 1)
         want = ref.get(0).reshape(4, W, 3)

@@ -195,6 +195,34 @@ def bench_reference(args, wl):
     print(json.dumps(line), flush=True)
 
 
+class RankSync:
+    """Barriers and max-over-ranks of the replicas (one process per GPU under
+    torchrun; gloo on the host, no data-path collective); no-ops for one rank."""
+
+    def __init__(self, world):
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            if not dist.is_initialized():
+                dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x):
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+
 class FlushBuffer:
     """Writes 256 MB of device memory (twice the 126 MB L2) before a step."""
 
@@ -337,6 +365,7 @@ def bench_gpu(args, wl):
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
     if not gb.device_available():
         raise SystemExit("bench: no usable CUDA device")
+    sync = RankSync(world)
     W, H = wl["W"], wl["H"]
     (v, t, m), cam = scene_and_camera(wl)
     scene = gb.RTScene(v, t, m).build_bvh()
@@ -355,16 +384,21 @@ def bench_gpu(args, wl):
     for _ in range(warm):
         r.render_frames(scene, cam, 1, stats=True)
     with ClockSampler(0) as clk:
+        sync.barrier()
         phases, rays, paths, launches = timed_frames(r, scene, cam, args.steps, flush)
+        sync.barrier()
     clocks = clk.summary()
-    total_ms = phases["ms_total"]
+    # replicas: every rank renders the same frames; the job's time is the slowest rank's
+    total_ms = sync.max(phases["ms_total"])
     value = paths / (total_ms / 1e3) / 1e6
 
     # e2e through the public call with a host result buffer (D2H of the image each step)
+    sync.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         r.render(scene, cam, stats=False)
-    e2e_s = time.perf_counter() - t0
+    e2e_s = sync.max(time.perf_counter() - t0)
+    sync.barrier()
     e2e = paths / e2e_s / 1e6
 
     trace_bytes, cst = walk_bytes(r, scene, cam, args.traversal)

@@ -81,3 +81,27 @@ def test_shard_rows_cover_the_image():
             assert max(r for _, r in parts) - min(r for _, r in parts) <= 1
     with pytest.raises(ValueError):
         sharding.shard_rows(10, 2, 2)
+
+
+def _sync_worker(rank, world, port, out_dir):
+    import sys
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import bench
+    s = bench.RankSync(world)
+    s.barrier()
+    m = s.max(10.0 + rank)  # each rank's time; the job's is the slowest
+    s.barrier()
+    with open(os.path.join(out_dir, f"max{rank}.txt"), "w") as f:
+        f.write(repr(m))
+    dist.destroy_process_group()
+
+
+def test_bench_rank_sync_takes_the_slowest_rank(tmp_path):
+    """bench.py's replicas time the job by the slowest rank (barriers around
+    the timed steps, max over ranks), here with two gloo ranks on the CPU."""
+    import torch.multiprocessing as mp
+    mp.spawn(_sync_worker, args=(2, _free_port(), str(tmp_path)), nprocs=2, join=True)
+    for r in (0, 1):
+        assert float((tmp_path / f"max{r}.txt").read_text()) == 11.0

@@ -865,11 +865,14 @@ enum : uint32_t { kIdle = 0, kPathExt = 1, kPathShadow = 2 };
 
 // walk steps of the tail kernel between two refill checks: a lane whose walk
 // ends early waits for the others, and the warp then shades its finished
-// paths together.  Measured in Mpaths/s on interior / Cornell: 1: 154.4 /
-// 144.2, 4: 157.5 / 158.7, 16: 161.1 / 171.4, 64: 162.3 / 189.1, 512: 156.7 /
-// 197.4 (the hall, depth 5, runs no tail kernel).  Three CTAs per SM (80
-// registers, 80 B of spill) against two (116 registers): interior 167.0 ->
-// 170.0, Cornell 195.6 -> 193.6 Mpaths/s.
+// paths together.  Measured in Mpaths/s on interior / Cornell before walks
+// were carried (the hall then ran no tail kernel): 1: 154.4 / 144.2, 4:
+// 157.5 / 158.7, 16: 161.1 / 171.4, 64: 162.3 / 189.1, 512: 156.7 / 197.4;
+// with carrying and 16-step walk batches (hall / interior / Cornell): 32:
+// 194.3 / 175.4 / 171.6, 64: 195.9 / 178.8 / 190.4, 128: 195.2 / 178.1 /
+// 192.7.  Three CTAs per SM (80 registers, some spill) against two (116
+// registers): interior 167.0 -> 170.0, Cornell 195.6 -> 193.6 Mpaths/s; four
+// (64 registers): hall 195.9 -> 194.6, Cornell 190.4 -> 183.1.
 __host__ __device__ constexpr int tail_steps() { return 64; }
 
 template <bool kCount, bool kWide>

@@ -107,7 +107,8 @@ struct FrameArgs {
 
 struct RenderBuffers {
   Wave wave[2];
-  float4* hit;          // t, tri bits, u, v (t < 0: miss)
+  float4* hit;          // t, tri bits, u, v (t -1: miss, -2: the walk was carried on); one per wave
+                        // path, then one per walk resumed from the previous launch's carry records
   float4* sh[2];        // connection queues (bounce parity), 3 float4 per entry:
                         // {origin, slot} {dir, maxDist} {weighted contribution}
   float4* res;          // per slot: acc.xyz, n bits

@@ -301,7 +301,7 @@ def issue_side(name, trace_ms, rays_per_frame, sm_mhz):
             "static_source": src + " (instructions per ray and lanes per instruction; the rest measured in this run)"}
 
 
-def measure_workload(gb, name, steps, warmup, flush, peak):
+def measure_workload(gb, name, steps, warmup, flush, peak, sm_mhz=None):
     """One benchmark configuration on its own renderer: `steps` timed frames
     (budgeted frames for the adaptive one, after its uniform frames), the
     whole image (all its frames) timed once, and the walks' work rate."""
@@ -335,24 +335,39 @@ def measure_workload(gb, name, steps, warmup, flush, peak):
            "walk_work_rate": {"bytes_per_frame": int(tb), "achieved_GBs": round(tb / (trace_ms / 1e3) / 1e9, 1),
                               "frac_of_hbm": round(tb / (trace_ms / 1e3) / 1e9 / peak, 4)} if trace_ms else None}
     if name == "hall_adaptive":
-        out["filter"] = filter_roofline(ph, steps, wl["W"] * wl["H"], peak, int(params["filter_radius"]))
+        out["filter"] = filter_roofline(ph, steps, wl["W"] * wl["H"], peak, int(params["filter_radius"]), sm_mhz)
     r.close()
     scene.close()
     return out
 
 
-def filter_roofline(phases, steps, np_, peak, radius):
-    """Bilateral filter of a budgeted frame against its compulsory traffic: the colour,
-    position and normal planes read (12 B per pixel each) and 12 B per pixel written."""
+FILTER_PROFILE = "profiles/k_bilateral_tile_hall_adaptive_1280x720.md"
+
+
+def filter_roofline(phases, steps, np_, peak, radius, sm_mhz):
+    """Bilateral filter of a budgeted frame.  It is bound by instruction issue
+    (the per-tap weights): warp instructions per pixel from a one-kernel ncu
+    capture of the same pass (static, the file is named) x this frame's pixels
+    over the issue slots of its measured time at the sampled SM clock.  Beside
+    it, the HBM work rate of its compulsory traffic (the colour, position and
+    normal planes read, 12 B per pixel each, and 12 B per pixel written)."""
     ms = phases["ms_filter"] / steps
     if ms <= 0:
         return None
     planes = 3
     compulsory = (planes * 12 + 12) * np_
     gbs = compulsory / (ms / 1e3) / 1e9
-    return {"kernel": "k_bilateral_tile", "bound": "hbm", "ms_per_frame": round(ms, 4),
-            "compulsory_bytes": compulsory, "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(gbs / peak, 4), "taps_per_pixel": (2 * radius + 1) ** 2,
+    prof = read_profile(FILTER_PROFILE) or {}
+    issue = None
+    if prof.get("warp_inst_per_pixel") and sm_mhz:
+        slots = SMS * SCHEDULERS * sm_mhz * 1e6 * ms / 1e3
+        issue = {"frac": round(prof["warp_inst_per_pixel"] * np_ / slots, 4),
+                 "warp_inst_per_pixel": prof["warp_inst_per_pixel"],
+                 "static_source": FILTER_PROFILE + " (instructions per pixel at radius 4; the rest measured in this run)"}
+    return {"kernel": "k_bilateral_tile", "bound": "issue", "ms_per_frame": round(ms, 4), "issue": issue,
+            "hbm_work_rate": {"compulsory_bytes": compulsory, "achieved": round(gbs, 1), "peak": peak,
+                              "unit": "GB/s", "frac": round(gbs / peak, 4)},
+            "taps_per_pixel": (2 * radius + 1) ** 2,
             "algorithmic_bytes_naive": (2 * radius + 1) ** 2 * planes * 12 * np_}
 
 
@@ -429,7 +444,7 @@ def bench_gpu(args, wl):
         for name in WORKLOADS:
             if name != args.workload:
                 steps = 24 if name == "hall_adaptive" else max(4, min(args.steps, 10))
-                others[name] = measure_workload(gb, name, steps, 2, flush, peak)
+                others[name] = measure_workload(gb, name, steps, 2, flush, peak, clocks.get("sm_mhz"))
         extras["other_configs"] = others
 
     cpu = None
